@@ -1,0 +1,44 @@
+// Host-side declarations of the field-kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "pic_common.cuh"
+
+namespace pic {
+
+struct GridInfo {
+  int dim;
+  int n[3];
+  int ng;
+  int periodic[3];
+};
+
+// extended-stencil coefficients of Faraday_kernel (faraday_mink.hpp:25-69)
+template <typename real>
+struct Stencil {
+  real deltax, deltay, betaxy, betayx, deltaz, betaxz, betazx, betayz, betazy;
+};
+
+template <typename real>
+cudaError_t launch_faraday(const GridInfo& g, FieldView<real> EB, real c1, real c2,
+                           const Stencil<real>& st, bool yee, cudaStream_t s);
+template <typename real>
+cudaError_t launch_ampere(const GridInfo& g, FieldView<real> EB, FieldView<real> J, real c1,
+                          real c2, real jcoeff, real ppc0, bool curl, bool cur, bool fill,
+                          cudaStream_t s);
+template <typename real>
+cudaError_t launch_sync_currents(const GridInfo& g, FieldView<real> J, cudaStream_t s);
+template <typename real>
+cudaError_t launch_fill_ghosts(const GridInfo& g, FieldView<real> f, int c0, int c1,
+                               cudaStream_t s);
+template <typename real>
+cudaError_t launch_filter(const GridInfo& g, FieldView<real> J, FieldView<real> buff, int npasses,
+                          cudaStream_t s);
+template <typename real>
+cudaError_t launch_zero3(const GridInfo& g, FieldView<real> f, cudaStream_t s);
+template <typename real>
+cudaError_t launch_energy(const GridInfo& g, FieldView<real> EB, double dx, double* out,
+                          cudaStream_t s);
+
+}  // namespace pic

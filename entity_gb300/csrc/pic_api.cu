@@ -1,0 +1,612 @@
+// C ABI of the particle-in-cell hot path: argument validation, dispatch to
+// the templated kernels by (dimension, shape order, precision), the device
+// error word, and the context's persistent scratch.
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <utility>
+#include <vector>
+#include <cstring>
+#include <cuda_runtime.h>
+
+#include "../../include/entity_pic.h"
+#include "fields.cuh"
+#include "push_deposit.cuh"
+#include "sort.cuh"
+
+struct pic_ctx {
+  pic_grid             grid;
+  unsigned long long*  d_err     = nullptr;  // 4 counters
+  double*              d_energy  = nullptr;  // 2
+  // sort scratch (grown on demand)
+  void*                sort_buf  = nullptr;
+  size_t               sort_bytes = 0;
+  // phase timers: recorded event pairs per phase, resolved on read
+  bool                                            timers_on = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> intervals[PIC_NPHASES];
+  cudaEvent_t                                     open_start[PIC_NPHASES] = {};
+  std::vector<cudaEvent_t>                        event_pool;
+};
+
+namespace {
+
+using pic::FieldView;
+using pic::GridInfo;
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? PIC_OK : PIC_ERR_CUDA; }
+
+int min_ghosts(int order) { return order == 0 ? 1 : (order + 1) / 2 + 1; }
+
+int validate_grid(const pic_grid* g) {
+  if (!g) return PIC_ERR_ARG;
+  if (g->dim != 2 && g->dim != 3) return PIC_ERR_UNSUPPORTED;
+  if (g->order < 0 || g->order > 3) return PIC_ERR_UNSUPPORTED;
+  if (g->real_bytes != 4 && g->real_bytes != 8) return PIC_ERR_UNSUPPORTED;
+  if (g->ng < min_ghosts(g->order)) return PIC_ERR_ARG;
+  for (int d = 0; d < g->dim; ++d) {
+    if (g->n[d] < 2 * g->ng) return PIC_ERR_ARG;
+    for (int s = 0; s < 2; ++s)
+      if (g->prtl_bc[d][s] < PIC_BC_PERIODIC || g->prtl_bc[d][s] > PIC_BC_AXIS) return PIC_ERR_ARG;
+  }
+  if (g->dim == 2 && g->n[2] != 1) return PIC_ERR_ARG;
+  for (int k = 0; k < 4; ++k) {
+    if (g->em_stride[k] <= 0 || g->cur_stride[k] <= 0) return PIC_ERR_ARG;
+  }
+  // cell and key indices are 32-bit
+  const int64_t cells = (int64_t)g->n[0] * g->n[1] * (g->dim == 3 ? g->n[2] : 1);
+  if (cells >= (int64_t)1 << 30) return PIC_ERR_UNSUPPORTED;
+  return PIC_OK;
+}
+
+GridInfo ginfo(const pic_ctx* c) {
+  GridInfo g;
+  g.dim = c->grid.dim;
+  g.ng  = c->grid.ng;
+  for (int d = 0; d < 3; ++d) {
+    g.n[d]        = c->grid.n[d];
+    g.periodic[d] = d < c->grid.dim ? c->grid.fld_periodic[d] : 0;
+  }
+  return g;
+}
+
+template <typename real>
+FieldView<real> em_view(const pic_ctx* c, const void* p) {
+  return FieldView<real>{ (real*)p, c->grid.em_stride[0], c->grid.em_stride[1], c->grid.em_stride[2],
+                          c->grid.em_stride[3] };
+}
+template <typename real>
+FieldView<real> cur_view(const pic_ctx* c, const void* p) {
+  return FieldView<real>{ (real*)p, c->grid.cur_stride[0], c->grid.cur_stride[1],
+                          c->grid.cur_stride[2], c->grid.cur_stride[3] };
+}
+
+cudaStream_t strm(void* s) { return (cudaStream_t)s; }
+
+int validate_species(const pic_ctx* c, const pic_species* sp, bool need_prev) {
+  if (!sp) return PIC_ERR_ARG;
+  if (sp->npart < 0) return PIC_ERR_ARG;
+  if (sp->maxnpart > 0 && sp->npart > sp->maxnpart) return PIC_ERR_ARG;
+  if (sp->npart >= ((int64_t)1 << 31)) return PIC_ERR_UNSUPPORTED;
+  if (sp->npart == 0) return PIC_OK;
+  if (!sp->i1 || !sp->i2 || !sp->dx1 || !sp->dx2 || !sp->ux1 || !sp->ux2 || !sp->ux3 ||
+      !sp->weight || !sp->tag)
+    return PIC_ERR_ARG;
+  if (c->grid.dim == 3 && (!sp->i3 || !sp->dx3)) return PIC_ERR_ARG;
+  if (need_prev) {
+    if (!sp->i1_prev || !sp->i2_prev || !sp->dx1_prev || !sp->dx2_prev) return PIC_ERR_ARG;
+    if (c->grid.dim == 3 && (!sp->i3_prev || !sp->dx3_prev)) return PIC_ERR_ARG;
+  }
+  if (sp->pusher < PIC_PUSHER_NONE || sp->pusher > PIC_PUSHER_PHOTON) return PIC_ERR_ARG;
+  return PIC_OK;
+}
+
+pic::SpeciesPtrs sptrs(const pic_species* sp) {
+  pic::SpeciesPtrs s;
+  s.i1 = sp->i1;
+  s.i2 = sp->i2;
+  s.i3 = sp->i3;
+  s.i1p = sp->i1_prev;
+  s.i2p = sp->i2_prev;
+  s.i3p = sp->i3_prev;
+  s.dx1 = sp->dx1;
+  s.dx2 = sp->dx2;
+  s.dx3 = sp->dx3;
+  s.dx1p = sp->dx1_prev;
+  s.dx2p = sp->dx2_prev;
+  s.dx3p = sp->dx3_prev;
+  s.ux1 = sp->ux1;
+  s.ux2 = sp->ux2;
+  s.ux3 = sp->ux3;
+  s.w = sp->weight;
+  s.tag = sp->tag;
+  s.npart = sp->npart;
+  s.mass = sp->mass;
+  s.charge = sp->charge;
+  s.pusher = sp->pusher;
+  return s;
+}
+
+template <typename real>
+cudaError_t pd_dispatch(const pic_ctx* c, const pic::PDArgs<real>& a, int mode, bool photon,
+                        cudaStream_t s) {
+  const int D = c->grid.dim, O = c->grid.order;
+#define PIC_PD_CASE(DD, OO) \
+  if (D == DD && O == OO) return pic::launch_push_deposit<DD, OO, real>(a, mode, photon, s);
+  PIC_PD_CASE(2, 0)
+  PIC_PD_CASE(2, 1)
+  PIC_PD_CASE(2, 2)
+  PIC_PD_CASE(2, 3)
+  PIC_PD_CASE(3, 0)
+  PIC_PD_CASE(3, 1)
+  PIC_PD_CASE(3, 2)
+  PIC_PD_CASE(3, 3)
+#undef PIC_PD_CASE
+  return cudaErrorInvalidValue;
+}
+
+template <typename real>
+int run_pd(pic_ctx* c, const pic_species* sp, const void* EB, void* J, double dt, double omegaB0,
+           double dx, int mode, bool write_prev, cudaStream_t s) {
+  pic::PDArgs<real> a;
+  a.sp = sptrs(sp);
+  for (int d = 0; d < 3; ++d) {
+    a.pc.n[d]     = c->grid.n[d];
+    a.pc.bc[d][0] = c->grid.prtl_bc[d][0];
+    a.pc.bc[d][1] = c->grid.prtl_bc[d][1];
+  }
+  a.pc.ng = c->grid.ng;
+  a.EB    = em_view<real>(c, EB);
+  a.J     = cur_view<real>(c, J);
+  a.dt    = (real)dt;
+  a.dx    = (real)dx;
+  // normalized_dt_half = HALF * (charge / mass) * omegaB0 * dt with the float
+  // charge/mass of the species (src/kernels/pushers/sr.hpp:111)
+  const bool  photon = sp->pusher == PIC_PUSHER_PHOTON;
+  const float qm     = photon ? 0.0f : sp->charge / sp->mass;
+  a.ndth             = (real)0.5 * (real)qm * (real)omegaB0 * (real)dt;
+  a.inv_dt           = (real)1 / (real)dt;
+  a.charge           = (real)sp->charge;
+  a.vay              = sp->pusher == PIC_PUSHER_VAY;
+  a.write_prev       = write_prev ? 1 : 0;
+  a.err              = c->d_err;
+  return cuda_status(pd_dispatch<real>(c, a, mode, photon, s));
+}
+
+template <typename real>
+int zero_J(pic_ctx* c, void* J, cudaStream_t s) {
+  return cuda_status(pic::launch_zero3<real>(ginfo(c), cur_view<real>(c, J), s));
+}
+
+bool is_f64(const pic_ctx* c) { return c->grid.real_bytes == 8; }
+
+}  // namespace
+
+namespace pic {
+static std::atomic<long long> g_launches{ 0 };
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace pic
+
+extern "C" {
+
+int64_t pic_kernel_launches(void) { return (int64_t)pic::g_launches.load(std::memory_order_relaxed); }
+
+int pic_version(int32_t* abi_version, int32_t* built_sm) {
+  if (abi_version) *abi_version = PIC_ABI_VERSION;
+  if (built_sm) *built_sm = 103;
+  return PIC_OK;
+}
+
+const char* pic_status_string(int status) {
+  switch (status) {
+    case PIC_OK: return "ok";
+    case PIC_ERR_ARG: return "invalid argument";
+    case PIC_ERR_CUDA: return "CUDA runtime error";
+    case PIC_ERR_UNSUPPORTED: return "unsupported configuration";
+    case PIC_ERR_NOMEM: return "device allocation failed";
+    case PIC_ERR_DEVICE: return "device-side check failed";
+    default: return "unknown status";
+  }
+}
+
+int pic_create(const pic_grid* grid, pic_ctx** out) {
+  if (!out) return PIC_ERR_ARG;
+  *out    = nullptr;
+  int st  = validate_grid(grid);
+  if (st != PIC_OK) return st;
+  pic_ctx* c = new pic_ctx();
+  c->grid    = *grid;
+  if (cudaMalloc((void**)&c->d_err, sizeof(unsigned long long) * 4) != cudaSuccess ||
+      cudaMalloc((void**)&c->d_energy, sizeof(double) * 2) != cudaSuccess) {
+    if (c->d_err) cudaFree(c->d_err);
+    delete c;
+    return PIC_ERR_NOMEM;
+  }
+  if (cudaMemset(c->d_err, 0, sizeof(unsigned long long) * 4) != cudaSuccess) {
+    cudaFree(c->d_err);
+    cudaFree(c->d_energy);
+    delete c;
+    return PIC_ERR_CUDA;
+  }
+  *out = c;
+  return PIC_OK;
+}
+
+int pic_timers_reset(pic_ctx* c) {
+  if (!c) return PIC_ERR_ARG;
+  for (int p = 0; p < PIC_NPHASES; ++p) {
+    for (auto& iv : c->intervals[p]) {
+      c->event_pool.push_back(iv.first);
+      c->event_pool.push_back(iv.second);
+    }
+    c->intervals[p].clear();
+    if (c->open_start[p]) c->event_pool.push_back(c->open_start[p]);
+    c->open_start[p] = nullptr;
+  }
+  return PIC_OK;
+}
+
+int pic_destroy(pic_ctx* c) {
+  if (!c) return PIC_ERR_ARG;
+  cudaDeviceSynchronize();
+  pic_timers_reset(c);
+  for (auto e : c->event_pool) cudaEventDestroy(e);
+  cudaFree(c->d_err);
+  cudaFree(c->d_energy);
+  if (c->sort_buf) cudaFree(c->sort_buf);
+  delete c;
+  return PIC_OK;
+}
+
+int pic_timers_enable(pic_ctx* c, int32_t on) {
+  if (!c) return PIC_ERR_ARG;
+  c->timers_on = on != 0;
+  return PIC_OK;
+}
+
+int pic_timer_mark(pic_ctx* c, int32_t phase, int32_t is_end, void* stream) {
+  if (!c || phase < 0 || phase >= PIC_NPHASES) return PIC_ERR_ARG;
+  if (!c->timers_on) return PIC_OK;
+  cudaEvent_t ev;
+  if (!c->event_pool.empty()) {
+    ev = c->event_pool.back();
+    c->event_pool.pop_back();
+  } else if (cudaEventCreate(&ev) != cudaSuccess) {
+    return PIC_ERR_CUDA;
+  }
+  if (cudaEventRecord(ev, strm(stream)) != cudaSuccess) return PIC_ERR_CUDA;
+  if (!is_end) {
+    if (c->open_start[phase]) c->event_pool.push_back(c->open_start[phase]);
+    c->open_start[phase] = ev;
+  } else {
+    if (!c->open_start[phase]) {
+      c->event_pool.push_back(ev);
+      return PIC_ERR_ARG;
+    }
+    c->intervals[phase].emplace_back(c->open_start[phase], ev);
+    c->open_start[phase] = nullptr;
+  }
+  return PIC_OK;
+}
+
+int pic_timers_read(pic_ctx* c, double ms[PIC_NPHASES], int64_t count[PIC_NPHASES]) {
+  if (!c || !ms || !count) return PIC_ERR_ARG;
+  for (int p = 0; p < PIC_NPHASES; ++p) {
+    double tot = 0.0;
+    for (auto& iv : c->intervals[p]) {
+      if (cudaEventSynchronize(iv.second) != cudaSuccess) return PIC_ERR_CUDA;
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, iv.first, iv.second) != cudaSuccess) return PIC_ERR_CUDA;
+      tot += t;
+    }
+    ms[p]    = tot;
+    count[p] = (int64_t)c->intervals[p].size();
+  }
+  return PIC_OK;
+}
+
+int pic_get_grid(const pic_ctx* c, pic_grid* out) {
+  if (!c || !out) return PIC_ERR_ARG;
+  *out = c->grid;
+  return PIC_OK;
+}
+
+int pic_faraday(pic_ctx* c, void* EB, double coeff1, double coeff2, const double* st, void* stream) {
+  if (!c || !EB) return PIC_ERR_ARG;
+  bool yee = true;
+  if (st) {
+    for (int k = 0; k < 9; ++k) yee = yee && st[k] == 0.0;
+  }
+  if (is_f64(c)) {
+    pic::Stencil<double> s{};
+    if (st) s = { st[0], st[1], st[2], st[3], st[4], st[5], st[6], st[7], st[8] };
+    return cuda_status(pic::launch_faraday<double>(ginfo(c), em_view<double>(c, EB), coeff1, coeff2, s,
+                                                   yee, strm(stream)));
+  }
+  pic::Stencil<float> s{};
+  if (st)
+    s = { (float)st[0], (float)st[1], (float)st[2], (float)st[3], (float)st[4],
+          (float)st[5], (float)st[6], (float)st[7], (float)st[8] };
+  return cuda_status(pic::launch_faraday<float>(ginfo(c), em_view<float>(c, EB), (float)coeff1,
+                                                (float)coeff2, s, yee, strm(stream)));
+}
+
+int pic_ampere(pic_ctx* c, void* EB, double coeff1, double coeff2, void* stream) {
+  if (!c || !EB) return PIC_ERR_ARG;
+  if (is_f64(c))
+    return cuda_status(pic::launch_ampere<double>(ginfo(c), em_view<double>(c, EB), cur_view<double>(c, nullptr),
+                                                  coeff1, coeff2, 0.0, 1.0, true, false, false,
+                                                  strm(stream)));
+  return cuda_status(pic::launch_ampere<float>(ginfo(c), em_view<float>(c, EB), cur_view<float>(c, nullptr),
+                                               (float)coeff1, (float)coeff2, 0.f, 1.f, true, false,
+                                               false, strm(stream)));
+}
+
+int pic_currents_ampere(pic_ctx* c, void* EB, void* J, double coeff, double ppc0, void* stream) {
+  if (!c || !EB || !J) return PIC_ERR_ARG;
+  if (ppc0 == 0.0) return PIC_ERR_ARG;
+  if (is_f64(c))
+    return cuda_status(pic::launch_ampere<double>(ginfo(c), em_view<double>(c, EB), cur_view<double>(c, J), 0.0,
+                                                  0.0, coeff, ppc0, false, true, true, strm(stream)));
+  return cuda_status(pic::launch_ampere<float>(ginfo(c), em_view<float>(c, EB), cur_view<float>(c, J), 0.f, 0.f,
+                                               (float)coeff, (float)ppc0, false, true, true,
+                                               strm(stream)));
+}
+
+int pic_ampere_currents(pic_ctx* c, void* EB, void* J, double coeff1, double coeff2, double jcoeff,
+                        double ppc0, void* stream) {
+  if (!c || !EB) return PIC_ERR_ARG;
+  if (J && ppc0 == 0.0) return PIC_ERR_ARG;
+  const bool cur = J != nullptr;
+  if (is_f64(c))
+    return cuda_status(pic::launch_ampere<double>(ginfo(c), em_view<double>(c, EB), cur_view<double>(c, J),
+                                                  coeff1, coeff2, jcoeff, ppc0, true, cur, true,
+                                                  strm(stream)));
+  return cuda_status(pic::launch_ampere<float>(ginfo(c), em_view<float>(c, EB), cur_view<float>(c, J),
+                                               (float)coeff1, (float)coeff2, (float)jcoeff,
+                                               (float)ppc0, true, cur, true, strm(stream)));
+}
+
+int pic_push(pic_ctx* c, const pic_species* sp, const void* EB, double dt, double omegaB0,
+             double dx, void* stream) {
+  if (!c || !EB) return PIC_ERR_ARG;
+  int st = validate_species(c, sp, true);
+  if (st != PIC_OK) return st;
+  if (sp->npart == 0 || sp->pusher == PIC_PUSHER_NONE) return PIC_OK;
+  if (sp->pusher != PIC_PUSHER_PHOTON && sp->mass == 0.0f) return PIC_ERR_ARG;
+  if (is_f64(c))
+    return run_pd<double>(c, sp, EB, nullptr, dt, omegaB0, dx, pic::MODE_PUSH, true, strm(stream));
+  return run_pd<float>(c, sp, EB, nullptr, dt, omegaB0, dx, pic::MODE_PUSH, true, strm(stream));
+}
+
+int pic_deposit(pic_ctx* c, const pic_species* sp, int32_t nspecies, void* J, double dt, double dx,
+                void* stream) {
+  if (!c || !J || nspecies < 0 || (nspecies > 0 && !sp)) return PIC_ERR_ARG;
+  for (int k = 0; k < nspecies; ++k) {
+    int st = validate_species(c, sp + k, true);
+    if (st != PIC_OK) return st;
+  }
+  int st = is_f64(c) ? zero_J<double>(c, J, strm(stream)) : zero_J<float>(c, J, strm(stream));
+  if (st != PIC_OK) return st;
+  for (int k = 0; k < nspecies; ++k) {
+    const pic_species* s = sp + k;
+    // currents.h:75-78: skip pusher NONE, empty species, zero charge
+    if (s->pusher == PIC_PUSHER_NONE || s->npart == 0 || s->charge == 0.0f) continue;
+    st = is_f64(c) ? run_pd<double>(c, s, nullptr, J, dt, 0.0, dx, pic::MODE_DEPOSIT, false, strm(stream))
+                   : run_pd<float>(c, s, nullptr, J, dt, 0.0, dx, pic::MODE_DEPOSIT, false, strm(stream));
+    if (st != PIC_OK) return st;
+  }
+  return PIC_OK;
+}
+
+int pic_push_deposit(pic_ctx* c, const pic_species* sp, int32_t nspecies, const void* EB, void* J,
+                     double dt, double omegaB0, double dx, uint32_t flags, void* stream) {
+  if (!c || !EB || !J || nspecies < 0 || (nspecies > 0 && !sp)) return PIC_ERR_ARG;
+  const bool write_prev = (flags & PIC_PD_WRITE_PREV) != 0;
+  for (int k = 0; k < nspecies; ++k) {
+    int st = validate_species(c, sp + k, write_prev);
+    if (st != PIC_OK) return st;
+    if (sp[k].pusher != PIC_PUSHER_NONE && sp[k].pusher != PIC_PUSHER_PHOTON && sp[k].mass == 0.0f)
+      return PIC_ERR_ARG;
+  }
+  int st = PIC_OK;
+  if (!(flags & PIC_PD_NO_ZERO)) {
+    st = is_f64(c) ? zero_J<double>(c, J, strm(stream)) : zero_J<float>(c, J, strm(stream));
+    if (st != PIC_OK) return st;
+  }
+  for (int k = 0; k < nspecies; ++k) {
+    const pic_species* s = sp + k;
+    if (s->pusher == PIC_PUSHER_NONE || s->npart == 0) continue;
+    // a species that moves but carries no charge is pushed only
+    const int mode = (s->charge == 0.0f) ? pic::MODE_PUSH : pic::MODE_FUSED;
+    if (mode == pic::MODE_PUSH && !write_prev) {
+      // push-only kernels always store prev; without prev arrays use the
+      // fused kernel with zero charge semantics instead
+      st = is_f64(c) ? run_pd<double>(c, s, EB, J, dt, omegaB0, dx, pic::MODE_FUSED, false, strm(stream))
+                     : run_pd<float>(c, s, EB, J, dt, omegaB0, dx, pic::MODE_FUSED, false, strm(stream));
+    } else {
+      st = is_f64(c) ? run_pd<double>(c, s, EB, J, dt, omegaB0, dx, mode, write_prev, strm(stream))
+                     : run_pd<float>(c, s, EB, J, dt, omegaB0, dx, mode, write_prev, strm(stream));
+    }
+    if (st != PIC_OK) return st;
+  }
+  return PIC_OK;
+}
+
+int pic_sync_currents(pic_ctx* c, void* J, void* buff, void* stream) {
+  (void)buff;
+  if (!c || !J) return PIC_ERR_ARG;
+  if (is_f64(c)) return cuda_status(pic::launch_sync_currents<double>(ginfo(c), cur_view<double>(c, J), strm(stream)));
+  return cuda_status(pic::launch_sync_currents<float>(ginfo(c), cur_view<float>(c, J), strm(stream)));
+}
+
+int pic_filter_currents(pic_ctx* c, void* J, void* buff, int32_t npasses, void* stream) {
+  if (!c || !J || npasses < 0) return PIC_ERR_ARG;
+  if (npasses == 0) return PIC_OK;
+  if (!buff) return PIC_ERR_ARG;
+  if (is_f64(c))
+    return cuda_status(pic::launch_filter<double>(ginfo(c), cur_view<double>(c, J), cur_view<double>(c, buff),
+                                                  npasses, strm(stream)));
+  return cuda_status(pic::launch_filter<float>(ginfo(c), cur_view<float>(c, J), cur_view<float>(c, buff),
+                                               npasses, strm(stream)));
+}
+
+int pic_fill_ghosts(pic_ctx* c, void* field, int32_t is_em, int32_t c0, int32_t c1, void* stream) {
+  if (!c || !field) return PIC_ERR_ARG;
+  const int ncomp = is_em ? 6 : 3;
+  if (c0 < 0 || c1 > ncomp || c0 >= c1) return PIC_ERR_ARG;
+  if (is_f64(c)) {
+    auto v = is_em ? em_view<double>(c, field) : cur_view<double>(c, field);
+    return cuda_status(pic::launch_fill_ghosts<double>(ginfo(c), v, c0, c1, strm(stream)));
+  }
+  auto v = is_em ? em_view<float>(c, field) : cur_view<float>(c, field);
+  return cuda_status(pic::launch_fill_ghosts<float>(ginfo(c), v, c0, c1, strm(stream)));
+}
+
+int pic_field_energy(pic_ctx* c, const void* EB, double dx, double* out, void* stream) {
+  if (!c || !EB || !out) return PIC_ERR_ARG;
+  cudaStream_t s = strm(stream);
+  if (cudaMemsetAsync(c->d_energy, 0, sizeof(double) * 2, s) != cudaSuccess) return PIC_ERR_CUDA;
+  cudaError_t e = is_f64(c) ? pic::launch_energy<double>(ginfo(c), em_view<double>(c, EB), dx, c->d_energy, s)
+                            : pic::launch_energy<float>(ginfo(c), em_view<float>(c, EB), dx, c->d_energy, s);
+  if (e != cudaSuccess) return PIC_ERR_CUDA;
+  if (cudaMemcpyAsync(out, c->d_energy, sizeof(double) * 2, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
+int pic_get_device_errors(pic_ctx* c, int64_t out[4], int32_t reset, void* stream) {
+  if (!c || !out) return PIC_ERR_ARG;
+  cudaStream_t       s = strm(stream);
+  unsigned long long h[4];
+  if (cudaMemcpyAsync(h, c->d_err, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return PIC_ERR_CUDA;
+  for (int k = 0; k < 4; ++k) out[k] = (int64_t)h[k];
+  if (reset) {
+    if (cudaMemsetAsync(c->d_err, 0, sizeof(h), s) != cudaSuccess) return PIC_ERR_CUDA;
+  }
+  return PIC_OK;
+}
+
+int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, void* stream) {
+  if (!c) return PIC_ERR_ARG;
+  const bool skip_prev = (flags & PIC_SORT_SKIP_PREV) != 0;
+  int        st        = validate_species(c, sp, !skip_prev);
+  if (st != PIC_OK) return st;
+  const bool remove_dead = (flags & PIC_SORT_REMOVE_DEAD) != 0;
+  const bool spatial     = (flags & PIC_SORT_SPATIAL) != 0;
+  cudaStream_t  s        = strm(stream);
+  const int64_t np       = sp->npart;
+  if (npart_out) *npart_out = np;
+  if (np == 0 || (!remove_dead && !spatial)) return PIC_OK;
+
+  const pic_grid& g     = c->grid;
+  const int64_t   cells = spatial ? (int64_t)g.n[0] * g.n[1] * (g.dim == 3 ? g.n[2] : 1) : 1;
+  const int64_t   nbins = cells + 1;  // + dead bin
+  // scratch layout (8-byte aligned pieces)
+  auto          al   = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t  b_key = al(4 * np), b_rank = al(4 * np), b_dead = al(np), b_drank = al(8 * np);
+  const size_t  b_cnt = al(4 * (nbins + 1)), b_off = al(8 * (nbins + 1)), b_perm = al(4 * np);
+  const size_t  b_ptmp = al(4 * np), b_big = al(4 * nbins), b_nbig = al(4);
+  const size_t  rb     = (size_t)g.real_bytes;
+  const size_t  b_tmp  = al(np * (rb > 4 ? rb : 4));
+  const size_t  need   = b_key + b_rank + b_dead + b_drank + b_cnt + b_off + b_perm + b_ptmp + b_big +
+                      b_nbig + b_tmp;
+  if (need > c->sort_bytes) {
+    if (c->sort_buf) cudaFree(c->sort_buf);
+    c->sort_buf   = nullptr;
+    c->sort_bytes = 0;
+    if (cudaMalloc(&c->sort_buf, need) != cudaSuccess) return PIC_ERR_NOMEM;
+    c->sort_bytes = need;
+  }
+  char*         base = (char*)c->sort_buf;
+  pic::SortArgs a;
+  a.i1 = sp->i1;
+  a.i2 = sp->i2;
+  a.i3 = sp->i3;
+  a.tag = sp->tag;
+  a.npart = np;
+  a.dim = g.dim;
+  a.n[0] = g.n[0];
+  a.n[1] = g.n[1];
+  a.n[2] = g.n[2];
+  a.spatial = spatial ? 1 : 0;
+  a.dead_bin = (int32_t)cells;
+  a.key = (int32_t*)base;
+  base += b_key;
+  a.rank = (int32_t*)base;
+  base += b_rank;
+  a.is_dead = (uint8_t*)base;
+  base += b_dead;
+  a.dead_rank = (int64_t*)base;
+  base += b_drank;
+  a.count = (int32_t*)base;
+  base += b_cnt;
+  a.off = (int64_t*)base;
+  base += b_off;
+  a.perm = (int32_t*)base;
+  base += b_perm;
+  a.perm_tmp = (int32_t*)base;
+  base += b_ptmp;
+  a.big = (int32_t*)base;
+  base += b_big;
+  a.nbig = (int32_t*)base;
+  base += b_nbig;
+  void* tmp = base;
+  a.err     = c->d_err;
+
+  int64_t     n_dead = 0;
+  cudaError_t e      = pic::sort_build_perm(a, &n_dead, s);
+  if (e != cudaSuccess) return PIC_ERR_CUDA;
+  const int32_t* perm = a.perm;
+#define PIC_APPLY(T, ptr)                                                    \
+  if ((e = pic::sort_apply<T>((T*)(ptr), tmp, perm, np, s)) != cudaSuccess) \
+    return PIC_ERR_CUDA;
+  PIC_APPLY(int32_t, sp->i1)
+  PIC_APPLY(int32_t, sp->i2)
+  PIC_APPLY(float, sp->dx1)
+  PIC_APPLY(float, sp->dx2)
+  if (g.dim == 3) {
+    PIC_APPLY(int32_t, sp->i3)
+    PIC_APPLY(float, sp->dx3)
+  }
+  if (!skip_prev) {
+    PIC_APPLY(int32_t, sp->i1_prev)
+    PIC_APPLY(int32_t, sp->i2_prev)
+    PIC_APPLY(float, sp->dx1_prev)
+    PIC_APPLY(float, sp->dx2_prev)
+    if (g.dim == 3) {
+      PIC_APPLY(int32_t, sp->i3_prev)
+      PIC_APPLY(float, sp->dx3_prev)
+    }
+  }
+  if (is_f64(c)) {
+    PIC_APPLY(double, sp->ux1)
+    PIC_APPLY(double, sp->ux2)
+    PIC_APPLY(double, sp->ux3)
+    PIC_APPLY(double, sp->weight)
+  } else {
+    PIC_APPLY(float, sp->ux1)
+    PIC_APPLY(float, sp->ux2)
+    PIC_APPLY(float, sp->ux3)
+    PIC_APPLY(float, sp->weight)
+  }
+  PIC_APPLY(int16_t, sp->tag)
+#undef PIC_APPLY
+  int64_t newn = np;
+  if (remove_dead) {
+    // particles_sort.cpp:175-191: alive tags on the front, dead on the tail
+    newn = np - n_dead;
+    if ((e = pic::set_tags(sp->tag, 0, newn, PIC_TAG_ALIVE, s)) != cudaSuccess) return PIC_ERR_CUDA;
+    if ((e = pic::set_tags(sp->tag, newn, np, PIC_TAG_DEAD, s)) != cudaSuccess) return PIC_ERR_CUDA;
+  }
+  unsigned long long h_err[4];
+  if (cudaMemcpyAsync(h_err, c->d_err, sizeof(h_err), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return PIC_ERR_CUDA;
+  if (npart_out) *npart_out = newn;
+  if (remove_dead) sp->npart = newn;
+  return h_err[pic::ERR_OUT_OF_GRID] ? PIC_ERR_DEVICE : PIC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,317 @@
+// Spatial sort and dead-particle removal of one species
+// (Particles::SortSpatially / RemoveDead,
+// src/framework/containers/particles_sort.cpp:103-253).
+//
+// The reference bins with Kokkos::BinSort (sort_within_bins = false), whose
+// order inside a cell is unspecified. This sort produces the stable order
+// (ascending original index inside every cell), which is one of the orders
+// the reference may produce, and is deterministic:
+//   1. key per particle (PositionToTileIndex, src/global/utils/sorting.h:
+//      119-135: (i1*n2 + i2)*n3 + i3; dead -> last bin) and an atomic count
+//      per bin whose return value is a provisional rank;
+//   2. exclusive scan of the counts -> bin offsets;
+//   3. scatter of indices; dead particles get their rank from a scan so the
+//      (possibly huge) dead bin is placed in order directly;
+//   4. every alive bin's index list is sorted ascending (one thread per bin up
+//      to 32 entries, one block per larger bin);
+//   5. every particle array is gathered through the permutation.
+#include <cuda_runtime.h>
+
+#include "sort.cuh"
+
+namespace pic {
+
+namespace {
+
+constexpr int kScanThreads = 512;
+constexpr int kScanItems   = 8;
+constexpr int kScanTile    = kScanThreads * kScanItems;
+
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T* sh, T& total) {
+  // warp inclusive scan
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  T         x    = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    T         s  = lane < nw ? sh[lane] : (T)0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < nw) sh[lane] = s;
+  }
+  __syncthreads();
+  const T warp_off = wid > 0 ? sh[wid - 1] : (T)0;
+  total            = sh[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}
+
+// per-tile sums of in[0..n)
+template <typename Tin, typename T>
+__global__ void k_tile_sums(const Tin* in, int64_t n, T* sums) {
+  __shared__ T  sh[32];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  T             s    = 0;
+#pragma unroll
+  for (int it = 0; it < kScanItems; ++it) {
+    const int64_t i = base + (int64_t)it * kScanThreads + threadIdx.x;
+    if (i < n) s += (T)in[i];
+  }
+  T total;
+  block_exclusive_scan<T>(s, sh, total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// exclusive scan of one tile with a carried-in offset per tile
+template <typename Tin, typename T>
+__global__ void k_tile_scan(const Tin* in, int64_t n, const T* tile_off, T* out) {
+  __shared__ T  sh[32];
+  __shared__ T  carry;
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  if (threadIdx.x == 0) carry = tile_off ? tile_off[blockIdx.x] : (T)0;
+  __syncthreads();
+  // each thread owns kScanItems consecutive elements
+  T         v[kScanItems];
+  T         s  = 0;
+  const int t0 = threadIdx.x * kScanItems;
+#pragma unroll
+  for (int it = 0; it < kScanItems; ++it) {
+    const int64_t i = base + t0 + it;
+    v[it]           = i < n ? (T)in[i] : (T)0;
+    s += v[it];
+  }
+  T total;
+  T pre = block_exclusive_scan<T>(s, sh, total) + carry;
+#pragma unroll
+  for (int it = 0; it < kScanItems; ++it) {
+    const int64_t i = base + t0 + it;
+    if (i < n) out[i] = pre;
+    pre += v[it];
+  }
+}
+
+}  // namespace
+
+// exclusive scan (out may alias in only through separate buffers)
+template <typename Tin, typename T>
+cudaError_t exclusive_scan(const Tin* in, int64_t n, T* out, ScanScratch<T>& scr, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t tiles = (n + kScanTile - 1) / kScanTile;
+  if (tiles == 1) {
+    PIC_KL(k_tile_scan<Tin, T><<<1, kScanThreads, 0, s>>>(in, n, (const T*)nullptr, out));
+    return cudaGetLastError();
+  }
+  T* sums = scr.get(tiles * 2 + 2, s);
+  if (!sums) return cudaErrorMemoryAllocation;
+  T* offs = sums + tiles + 1;
+  PIC_KL(k_tile_sums<Tin, T><<<(unsigned)tiles, kScanThreads, 0, s>>>(in, n, sums));
+  // recursive scan of the tile sums (depth log_4096(n))
+  ScanScratch<T> sub;
+  cudaError_t    e = exclusive_scan<T, T>(sums, tiles, offs, sub, s);
+  if (e != cudaSuccess) {
+    sub.release(s);
+    return e;
+  }
+  PIC_KL(k_tile_scan<Tin, T><<<(unsigned)tiles, kScanThreads, 0, s>>>(in, n, offs, out));
+  e = cudaGetLastError();
+  sub.release(s);
+  return e;
+}
+
+template cudaError_t exclusive_scan<int32_t, int64_t>(const int32_t*, int64_t, int64_t*,
+                                                      ScanScratch<int64_t>&, cudaStream_t);
+template cudaError_t exclusive_scan<uint8_t, int64_t>(const uint8_t*, int64_t, int64_t*,
+                                                      ScanScratch<int64_t>&, cudaStream_t);
+template cudaError_t exclusive_scan<int64_t, int64_t>(const int64_t*, int64_t, int64_t*,
+                                                      ScanScratch<int64_t>&, cudaStream_t);
+
+namespace {
+
+// 1. keys + counts + provisional rank
+__global__ void k_keys(SortArgs a) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.npart; p += stride) {
+    const short tag = a.tag[p];
+    int32_t     key;
+    if (tag != PIC_TAG_ALIVE) {
+      key = a.dead_bin;
+    } else if (!a.spatial) {
+      key = 0;
+    } else {
+      const int i1 = a.i1[p], i2 = a.i2[p], i3 = a.dim == 3 ? a.i3[p] : 0;
+      const bool ok = (i1 >= 0 && i1 < a.n[0] && i2 >= 0 && i2 < a.n[1] &&
+                       (a.dim == 2 || (i3 >= 0 && i3 < a.n[2])));
+      if (!ok) {
+        atomicAdd(a.err + ERR_OUT_OF_GRID, 1ull);
+        key = a.dead_bin;  // kept after the alive particles, tag untouched
+      } else if (a.dim == 2) {
+        key = i1 * a.n[1] + i2;
+      } else {
+        key = (i1 * a.n[1] + i2) * a.n[2] + i3;
+      }
+    }
+    a.key[p]        = key;
+    a.is_dead[p]    = (uint8_t)(key == a.dead_bin);
+    a.rank[p]       = atomicAdd(a.count + key, 1);
+  }
+}
+
+// 3. scatter of particle indices into their bins
+__global__ void k_scatter(SortArgs a) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.npart; p += stride) {
+    const int32_t key = a.key[p];
+    int64_t       pos;
+    if (key == a.dead_bin) {
+      pos = a.off[key] + a.dead_rank[p];
+    } else if (!a.spatial) {
+      pos = p - a.dead_rank[p];  // alive before p, in order
+    } else {
+      pos = a.off[key] + a.rank[p];
+    }
+    a.perm[pos] = (int32_t)p;
+  }
+}
+
+// 4a. per-bin ascending order, small bins
+__global__ void k_fix_small(SortArgs a) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < a.dead_bin; b += stride) {
+    const int64_t lo = a.off[b], hi = a.off[b + 1];
+    const int64_t m  = hi - lo;
+    if (m <= 1) continue;
+    if (m > 32) {
+      const int slot = atomicAdd(a.nbig, 1);
+      a.big[slot]    = (int32_t)b;
+      continue;
+    }
+    int32_t v[32];
+    for (int q = 0; q < m; ++q) v[q] = a.perm[lo + q];
+    for (int q = 1; q < m; ++q) {
+      const int32_t x = v[q];
+      int           r = q - 1;
+      while (r >= 0 && v[r] > x) {
+        v[r + 1] = v[r];
+        --r;
+      }
+      v[r + 1] = x;
+    }
+    for (int q = 0; q < m; ++q) a.perm[lo + q] = v[q];
+  }
+}
+
+// 4b. large bins: rank by counting, one block per bin (O(m^2 / threads))
+__global__ void k_fix_big(SortArgs a) {
+  const int     b  = a.big[blockIdx.x];
+  const int64_t lo = a.off[b], hi = a.off[b + 1];
+  const int64_t m  = hi - lo;
+  for (int64_t q = threadIdx.x; q < m; q += blockDim.x) {
+    const int32_t x = a.perm[lo + q];
+    int64_t       r = 0;
+    for (int64_t z = 0; z < m; ++z) r += (a.perm[lo + z] < x);
+    a.perm_tmp[lo + r] = x;
+  }
+  __syncthreads();
+  for (int64_t q = threadIdx.x; q < m; q += blockDim.x) a.perm[lo + q] = a.perm_tmp[lo + q];
+}
+
+template <typename T>
+__global__ void k_gather(const T* __restrict__ src, T* __restrict__ dst, const int32_t* perm,
+                         int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    dst[i] = src[perm[i]];
+  }
+}
+
+__global__ void k_set_tags(int16_t* tag, int64_t lo, int64_t hi, int16_t value) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < hi; i += stride) {
+    tag[i] = value;
+  }
+}
+
+dim3 grid_n(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 152 * 64) b = 152 * 64;
+  if (b < 1) b = 1;
+  return dim3((unsigned)b);
+}
+
+}  // namespace
+
+cudaError_t sort_build_perm(SortArgs a, int64_t* n_dead_out, cudaStream_t s) {
+  cudaError_t e;
+  const int64_t nbins = (int64_t)a.dead_bin + 1;
+  e = cudaMemsetAsync(a.count, 0, sizeof(int32_t) * (nbins + 1), s);
+  if (e != cudaSuccess) return e;
+  PIC_KL(k_keys<<<grid_n(a.npart), 256, 0, s>>>(a));
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  ScanScratch<int64_t> scr;
+  e = exclusive_scan<int32_t, int64_t>(a.count, nbins + 1, a.off, scr, s);
+  scr.release(s);
+  if (e != cudaSuccess) return e;
+  int32_t n_dead = 0;
+  e = cudaMemcpyAsync(&n_dead, a.count + a.dead_bin, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  if (n_dead > 0) {
+    ScanScratch<int64_t> scr2;
+    e = exclusive_scan<uint8_t, int64_t>(a.is_dead, a.npart, a.dead_rank, scr2, s);
+    scr2.release(s);
+    if (e != cudaSuccess) return e;
+  } else if (!a.spatial) {
+    e = cudaMemsetAsync(a.dead_rank, 0, sizeof(int64_t) * a.npart, s);
+    if (e != cudaSuccess) return e;
+  }
+  PIC_KL(k_scatter<<<grid_n(a.npart), 256, 0, s>>>(a));
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (a.spatial && a.dead_bin > 0) {
+    e = cudaMemsetAsync(a.nbig, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess) return e;
+    PIC_KL(k_fix_small<<<grid_n(a.dead_bin), 256, 0, s>>>(a));
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    int32_t nbig = 0;
+    e = cudaMemcpyAsync(&nbig, a.nbig, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+    if (nbig > 0) {
+      PIC_KL(k_fix_big<<<(unsigned)nbig, 256, 0, s>>>(a));
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+  }
+  *n_dead_out = n_dead;
+  return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t sort_apply(T* arr, void* tmp, const int32_t* perm, int64_t n, cudaStream_t s) {
+  if (!arr || n <= 0) return cudaSuccess;
+  PIC_KL(k_gather<T><<<grid_n(n), 256, 0, s>>>(arr, (T*)tmp, perm, n));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(arr, tmp, sizeof(T) * n, cudaMemcpyDeviceToDevice, s);
+}
+
+template cudaError_t sort_apply<int32_t>(int32_t*, void*, const int32_t*, int64_t, cudaStream_t);
+template cudaError_t sort_apply<float>(float*, void*, const int32_t*, int64_t, cudaStream_t);
+template cudaError_t sort_apply<double>(double*, void*, const int32_t*, int64_t, cudaStream_t);
+template cudaError_t sort_apply<int16_t>(int16_t*, void*, const int32_t*, int64_t, cudaStream_t);
+
+cudaError_t set_tags(int16_t* tag, int64_t lo, int64_t hi, int16_t value, cudaStream_t s) {
+  if (hi <= lo) return cudaSuccess;
+  PIC_KL(k_set_tags<<<grid_n(hi - lo), 256, 0, s>>>(tag, lo, hi, value));
+  return cudaGetLastError();
+}
+
+}  // namespace pic

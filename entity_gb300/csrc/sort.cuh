@@ -1,0 +1,68 @@
+// Host-side declarations for the sort and scan kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pic_types.h"
+
+namespace pic {
+
+// stream-ordered scratch for the recursive levels of the scan
+template <typename T>
+struct ScanScratch {
+  T*      p   = nullptr;
+  int64_t cap = 0;
+  T* get(int64_t n, cudaStream_t s) {
+    if (n > cap) {
+      if (p) cudaFreeAsync(p, s);
+      p   = nullptr;
+      cap = 0;
+      if (cudaMallocAsync((void**)&p, sizeof(T) * n, s) != cudaSuccess) return nullptr;
+      cap = n;
+    }
+    return p;
+  }
+  void release(cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
+    p   = nullptr;
+    cap = 0;
+  }
+};
+
+template <typename Tin, typename T>
+cudaError_t exclusive_scan(const Tin* in, int64_t n, T* out, ScanScratch<T>& scr, cudaStream_t s);
+
+struct SortArgs {
+  // particle arrays
+  const int32_t *i1, *i2, *i3;
+  const int16_t *tag;
+  int64_t        npart;
+  int            dim;
+  int            n[3];
+  int            spatial;   // 1: cell key, 0: alive/dead only
+  int32_t        dead_bin;  // index of the last bin
+  // scratch
+  int32_t*  key;
+  int32_t*  rank;
+  uint8_t*  is_dead;
+  int64_t*  dead_rank;
+  int32_t*  count;  // dead_bin + 2 entries
+  int64_t*  off;    // dead_bin + 2 entries
+  int32_t*  perm;
+  int32_t*  perm_tmp;
+  int32_t*  big;
+  int32_t*  nbig;
+  unsigned long long* err;
+};
+
+// builds perm (new index -> old index); returns the dead count
+cudaError_t sort_build_perm(SortArgs a, int64_t* n_dead_out, cudaStream_t s);
+
+// arr[i] <- arr[perm[i]] through tmp (tmp holds >= n elements of T)
+template <typename T>
+cudaError_t sort_apply(T* arr, void* tmp, const int32_t* perm, int64_t n, cudaStream_t s);
+
+cudaError_t set_tags(int16_t* tag, int64_t lo, int64_t hi, int16_t value, cudaStream_t s);
+
+}  // namespace pic

@@ -1,0 +1,189 @@
+"""Python mirror of the reference's SR phase functions, driving the C ABI.
+
+Each function has the reference's name and argument meaning
+(srpic::Faraday, srpic::Ampere, srpic::CurrentsAmpere, srpic::ParticlePush,
+srpic::CurrentsDeposit, srpic::CurrentsFilter, Metadomain::SynchronizeFields,
+Metadomain::CommunicateFields, Metadomain::SortParticles; see
+include/entity_pic.h for the file:line of each) and raises PicError where the
+reference raises. Device memory is held in torch tensors; torch is only the
+allocator here, every computation runs in libentity_pic.so.
+"""
+import ctypes as C
+
+import torch
+
+from . import abi
+from .inputs import GridSpec, SpeciesArrays
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    return C.c_void_p(stream.cuda_stream)
+
+
+def make_grid(g: GridSpec) -> abi.PicGrid:
+    pg = abi.PicGrid()
+    pg.dim = g.dim
+    for d in range(3):
+        pg.n[d] = g.n[d] if d < g.dim else 1
+        pg.fld_periodic[d] = int(g.periodic[d]) if d < g.dim else 0
+        pg.prtl_bc[d][0] = g.prtl_bc[d][0]
+        pg.prtl_bc[d][1] = g.prtl_bc[d][1]
+    pg.ng = g.ng
+    pg.order = g.order
+    pg.real_bytes = g.real_bytes
+    s = g.strides()
+    for k in range(4):
+        pg.em_stride[k] = s[k]
+        pg.cur_stride[k] = s[k]
+    return pg
+
+
+def make_species(sp: SpeciesArrays, dim: int) -> abi.PicSpecies:
+    ps = abi.PicSpecies()
+    ps.i1, ps.i2 = _ptr(sp.i[0]), _ptr(sp.i[1])
+    ps.dx1, ps.dx2 = _ptr(sp.dx[0]), _ptr(sp.dx[1])
+    ps.i1_prev, ps.i2_prev = _ptr(sp.i_prev[0]), _ptr(sp.i_prev[1])
+    ps.dx1_prev, ps.dx2_prev = _ptr(sp.dx_prev[0]), _ptr(sp.dx_prev[1])
+    if dim == 3:
+        ps.i3, ps.dx3 = _ptr(sp.i[2]), _ptr(sp.dx[2])
+        ps.i3_prev, ps.dx3_prev = _ptr(sp.i_prev[2]), _ptr(sp.dx_prev[2])
+    ps.ux1, ps.ux2, ps.ux3 = _ptr(sp.u[0]), _ptr(sp.u[1]), _ptr(sp.u[2])
+    ps.weight = _ptr(sp.w)
+    ps.tag = _ptr(sp.tag)
+    ps.npart = sp.npart
+    ps.maxnpart = sp.tag.numel()
+    ps.mass = sp.mass
+    ps.charge = sp.charge
+    ps.pusher = sp.pusher
+    ps.index = sp.index
+    return ps
+
+
+class Context:
+    """One domain's context (pic_create / pic_destroy)."""
+
+    def __init__(self, g: GridSpec):
+        self.g = g
+        self.grid = make_grid(g)
+        h = C.c_void_p()
+        abi.call("pic_create", C.byref(self.grid), C.byref(h))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            abi.call("pic_destroy", self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- field solvers -----------------------------------------------------
+    def faraday(self, EB, coeff1, coeff2, stencil=None, stream=None):
+        st = None if stencil is None else (C.c_double * 9)(*stencil)
+        abi.call("pic_faraday", self.h, _ptr(EB), coeff1, coeff2, st, _stream_ptr(stream))
+
+    def ampere(self, EB, coeff1, coeff2, stream=None):
+        abi.call("pic_ampere", self.h, _ptr(EB), coeff1, coeff2, _stream_ptr(stream))
+
+    def currents_ampere(self, EB, J, coeff, ppc0, stream=None):
+        abi.call("pic_currents_ampere", self.h, _ptr(EB), _ptr(J), coeff, ppc0,
+                 _stream_ptr(stream))
+
+    def ampere_currents(self, EB, J, coeff1, coeff2, jcoeff, ppc0, stream=None):
+        abi.call("pic_ampere_currents", self.h, _ptr(EB), _ptr(J), coeff1, coeff2, jcoeff, ppc0,
+                 _stream_ptr(stream))
+
+    # --- particles ---------------------------------------------------------
+    def push(self, sp: SpeciesArrays, EB, dt, omegaB0, dx, stream=None):
+        ps = make_species(sp, self.g.dim)
+        abi.call("pic_push", self.h, C.byref(ps), _ptr(EB), dt, omegaB0, dx, _stream_ptr(stream))
+
+    def deposit(self, species, J, dt, dx, stream=None):
+        arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
+        abi.call("pic_deposit", self.h, arr, len(species), _ptr(J), dt, dx, _stream_ptr(stream))
+
+    def push_deposit(self, species, EB, J, dt, omegaB0, dx, flags=0, stream=None):
+        arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
+        abi.call("pic_push_deposit", self.h, arr, len(species), _ptr(EB), _ptr(J), dt, omegaB0,
+                 dx, flags, _stream_ptr(stream))
+
+    def sort(self, sp: SpeciesArrays, flags, stream=None):
+        ps = make_species(sp, self.g.dim)
+        n = C.c_int64(0)
+        st = abi.load().pic_sort(self.h, C.byref(ps), flags, C.byref(n), _stream_ptr(stream))
+        if st not in (abi.PIC_OK, abi.PIC_ERR_DEVICE):
+            abi.check("pic_sort", st)
+        sp.npart = n.value
+        return st
+
+    # --- currents ------------------------------------------------------------
+    def sync_currents(self, J, buff=None, stream=None):
+        abi.call("pic_sync_currents", self.h, _ptr(J), _ptr(buff), _stream_ptr(stream))
+
+    def filter_currents(self, J, buff, npasses, stream=None):
+        abi.call("pic_filter_currents", self.h, _ptr(J), _ptr(buff), npasses, _stream_ptr(stream))
+
+    def fill_ghosts(self, fld, is_em, c0, c1, stream=None):
+        abi.call("pic_fill_ghosts", self.h, _ptr(fld), int(is_em), c0, c1, _stream_ptr(stream))
+
+    # --- diagnostics ---------------------------------------------------------
+    def field_energy(self, EB, dx, stream=None):
+        out = (C.c_double * 2)()
+        abi.call("pic_field_energy", self.h, _ptr(EB), dx, out, _stream_ptr(stream))
+        return out[0], out[1]
+
+    def device_errors(self, reset=False, stream=None):
+        out = (C.c_int64 * 4)()
+        abi.call("pic_get_device_errors", self.h, out, int(reset), _stream_ptr(stream))
+        return list(out)
+
+    # --- phase timers ---------------------------------------------------------
+    def timers(self, on=True):
+        abi.call("pic_timers_enable", self.h, int(on))
+        abi.call("pic_timers_reset", self.h)
+
+    def read_timers(self):
+        ms = (C.c_double * 6)()
+        cnt = (C.c_int64 * 6)()
+        abi.call("pic_timers_read", self.h, ms, cnt)
+        return {name: (ms[k], cnt[k]) for k, name in enumerate(abi.PIC_PHASES)}
+
+    def step(self, species, EB, J, buff, prm: abi.PicStepParams, step, stream=None):
+        arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
+        abi.call("pic_srpic_step", self.h, arr, len(species), _ptr(EB), _ptr(J), _ptr(buff),
+                 C.byref(prm), step, _stream_ptr(stream))
+        for k, s in enumerate(species):
+            s.npart = arr[k].npart
+
+
+def step_params(g: GridSpec, *, cfl, ppc0, skindepth0, larmor0, nfilter=0, sort_interval=0,
+                clear_interval=100, correction=1.0, write_prev=False, fieldsolver=True,
+                deposit=True):
+    """Scales of SimulationParams (src/framework/parameters/parameters.cpp:47-78,
+    algorithms.cpp:18-27, minkowski.h:82-84) in real_t arithmetic."""
+    R = g.real
+    t = lambda v: torch.tensor(v, dtype=R)
+    dx = t(g.dx)
+    dxmin = dx / torch.sqrt(t(float(g.dim)))
+    dt = t(cfl) * dxmin
+    # V0 = sqrt_det_h (minkowski.h:144-152): SQR(dx) in 2D, CUBE(dx) in 3D
+    V0 = dx * dx if g.dim == 2 else dx * dx * dx
+    q0 = V0 / (t(ppc0) * (t(skindepth0) * t(skindepth0)))
+    B0 = t(1.0) / t(larmor0)
+    p = abi.PicStepParams()
+    p.dt, p.dx, p.omegaB0 = float(dt), float(dx), float(B0)
+    p.correction = float(t(correction))
+    p.q0, p.B0, p.V0, p.ppc0 = float(q0), float(B0), float(V0), float(t(ppc0))
+    p.nfilter, p.sort_interval, p.clear_interval = nfilter, sort_interval, clear_interval
+    p.fieldsolver_enabled, p.deposit_enabled = int(fieldsolver), int(deposit)
+    p.write_prev = int(write_prev)
+    return p

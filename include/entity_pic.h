@@ -1,0 +1,252 @@
+/*
+ * entity_pic.h — C ABI of the GB300 particle-in-cell hot path.
+ *
+ * One entry point per phase of the reference's SR step
+ * (SRPICEngine::step_forward, src/engines/srpic/srpic.hpp:65-188), taking
+ * plain device pointers, element strides and scalars. The caller owns every
+ * array (the reference's Kokkos Views pass `.data()`); the library never
+ * frees caller memory and allocates only inside pic_create and lazily in
+ * pic_sort (scratch that lives in the context).
+ *
+ * Errors: every entry point returns int (PIC_OK = 0, negative on failure) and
+ * never throws or traps. Device-side faults that the reference reports with
+ * Kokkos::abort (invalid particle tag, particle outside the grid after the
+ * boundary step) are counted in a device error word, read with
+ * pic_get_device_errors after the stream is synchronised.
+ *
+ * Threading: one host thread drives a context; calls are asynchronous on the
+ * given stream (NULL = legacy default stream).
+ *
+ * Paths in citations are relative to the entity repository.
+ */
+#ifndef ENTITY_PIC_H
+#define ENTITY_PIC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PIC_ABI_VERSION 1
+
+/* status codes */
+#define PIC_OK 0
+#define PIC_ERR_ARG -1         /* invalid argument (null pointer, bad size) */
+#define PIC_ERR_CUDA -2        /* a CUDA runtime call failed */
+#define PIC_ERR_UNSUPPORTED -3 /* configuration outside what is built */
+#define PIC_ERR_NOMEM -4       /* device allocation failed */
+#define PIC_ERR_DEVICE -5      /* a device-side check failed (see error word) */
+
+/* particle tags: ParticleTag, src/global/global.h:168-171 */
+#define PIC_TAG_DEAD 0
+#define PIC_TAG_ALIVE 1
+
+/* pusher kinds: ParticlePusher flags, src/global/enums.h */
+#define PIC_PUSHER_NONE 0
+#define PIC_PUSHER_BORIS 1
+#define PIC_PUSHER_VAY 2
+#define PIC_PUSHER_PHOTON 3
+
+/* particle boundary kinds: PusherBoundaries, src/kernels/pushers/context.h:124-178 */
+#define PIC_BC_PERIODIC 0
+#define PIC_BC_ABSORB 1
+#define PIC_BC_REFLECT 2
+#define PIC_BC_AXIS 3
+
+/* push/deposit flags */
+#define PIC_PD_WRITE_PREV 1u /* store i*_prev / dx*_prev like the reference pusher */
+#define PIC_PD_NO_ZERO 2u    /* do not zero J before depositing */
+
+/* sort flags */
+#define PIC_SORT_REMOVE_DEAD 1u /* Particles::RemoveDead before the spatial sort */
+#define PIC_SORT_SKIP_PREV 2u   /* leave i*_prev / dx*_prev arrays unpermuted */
+#define PIC_SORT_SPATIAL 4u     /* Particles::SortSpatially */
+
+/* Grid and build choices of a domain (Grid/Mesh, src/framework/domain/grid.h;
+ * N_GHOSTS and SHAPE_ORDER, src/global/global.h:130-136). Field element
+ * (i1, i2, i3, comp) with ghost-inclusive indices is at
+ * i1*s[0] + i2*s[1] + i3*s[2] + comp*s[3] (elements of real_bytes each);
+ * Kokkos LayoutLeft and LayoutRight are both expressible. */
+typedef struct {
+  int32_t dim;           /* 2 or 3 */
+  int32_t n[3];          /* active cells per dimension (n[2] = 1 in 2D) */
+  int32_t ng;            /* ghost layers */
+  int32_t order;         /* shape order 0 (zigzag) .. 3 */
+  int32_t real_bytes;    /* sizeof(real_t): 4 or 8 */
+  int32_t fld_periodic[3];
+  int32_t prtl_bc[3][2]; /* PIC_BC_* for (min, max) of each dimension */
+  int64_t em_stride[4];  /* strides of the 6-component EB (E at 0..2, B at 3..5) */
+  int64_t cur_stride[4]; /* strides of the 3-component J and buff */
+} pic_grid;
+
+/* One species as structure of arrays, field for field the reference's
+ * ParticleArrays (src/framework/containers/particles.h:47-71). ux*, weight are
+ * real_t; i*_prev / dx*_prev may be NULL when PIC_PD_WRITE_PREV is not set
+ * and the sort is asked to skip them. i3-arrays are unused in 2D. */
+typedef struct {
+  int32_t *i1, *i2, *i3;
+  int32_t *i1_prev, *i2_prev, *i3_prev;
+  float   *dx1, *dx2, *dx3;
+  float   *dx1_prev, *dx2_prev, *dx3_prev;
+  void    *ux1, *ux2, *ux3;
+  void    *weight;
+  int16_t *tag;
+  int64_t  npart;
+  int64_t  maxnpart;
+  float    mass;
+  float    charge;
+  int32_t  pusher; /* PIC_PUSHER_* */
+  int32_t  index;  /* species index (1-based as in the reference) */
+} pic_species;
+
+typedef struct pic_ctx pic_ctx;
+
+/* Library version and the build's compute capability (e.g. 103). */
+int pic_version(int32_t* abi_version, int32_t* built_sm);
+
+/* Human-readable status. */
+const char* pic_status_string(int status);
+
+/* Number of CUDA kernels this library has launched in the process so far
+ * (host-side counter; no device synchronisation). No reference counterpart:
+ * it lets a caller attribute launches to this library. */
+int64_t pic_kernel_launches(void);
+
+/* Creates a context for one domain: validates the grid, allocates the device
+ * error word. Replaces nothing in the reference (its Domain owns the Views). */
+int pic_create(const pic_grid* grid, pic_ctx** out);
+int pic_destroy(pic_ctx* ctx);
+
+/* Copy of the grid the context was created with. */
+int pic_get_grid(const pic_ctx* ctx, pic_grid* out);
+
+/* srpic::Faraday (src/engines/srpic/fieldsolvers.h:36-99) with
+ * Faraday_kernel (src/kernels/faraday_mink.hpp:71-166), fused with
+ * Metadomain::CommunicateFields(Comm::B) (metadomain_comm.cpp:204-367) for
+ * periodic dimensions. coeff1/coeff2 as the reference computes them in
+ * real_t; stencil = {deltax, deltay, betaxy, betayx, deltaz, betaxz, betazx,
+ * betayz, betazy} or NULL for Yee. */
+int pic_faraday(pic_ctx* ctx, void* EB, double coeff1, double coeff2,
+                const double* stencil, void* stream);
+
+/* srpic::Ampere (fieldsolvers.h:101-140), Ampere_kernel
+ * (src/kernels/ampere_mink.hpp:48-88); no ghost exchange (the reference
+ * exchanges E after CurrentsAmpere). */
+int pic_ampere(pic_ctx* ctx, void* EB, double coeff1, double coeff2, void* stream);
+
+/* srpic::CurrentsAmpere (fieldsolvers.h:142-200), CurrentsAmpere_kernel
+ * (ampere_mink.hpp:96-214): E += coeff*J, J /= ppc0, then
+ * CommunicateFields(Comm::E | Comm::J). */
+int pic_currents_ampere(pic_ctx* ctx, void* EB, void* J, double coeff, double ppc0,
+                        void* stream);
+
+/* Ampere + CurrentsAmpere + CommunicateFields(E|J) in one pass over the grid
+ * (srpic.hpp:155-166); with J == NULL only Ampere + CommunicateFields(E). */
+int pic_ampere_currents(pic_ctx* ctx, void* EB, void* J, double coeff1, double coeff2,
+                        double jcoeff, double ppc0, void* stream);
+
+/* srpic::ParticlePush (src/engines/srpic/particle_pusher.h:35-185) for one
+ * species: Pusher_kernel (src/kernels/pushers/sr.hpp:117-332), Minkowski,
+ * Boris / Vay / photon, with the particle boundaries of the grid. Always
+ * writes i*_prev / dx*_prev. */
+int pic_push(pic_ctx* ctx, const pic_species* sp, const void* EB, double dt,
+             double omegaB0, double dx, void* stream);
+
+/* srpic::CurrentsDeposit (src/engines/srpic/currents.h:64-87): zeroes J and
+ * deposits every species with DepositCurrents_kernel
+ * (src/kernels/currents_deposit.hpp:108-761) from the prev arrays. */
+int pic_deposit(pic_ctx* ctx, const pic_species* sp, int32_t nspecies, void* J, double dt,
+                double dx, void* stream);
+
+/* Fused ParticlePush + CurrentsDeposit for nspecies species: one pass reads
+ * each particle once, moves it and deposits its current; the previous
+ * position stays in registers (written out only with PIC_PD_WRITE_PREV).
+ * J is zeroed first unless PIC_PD_NO_ZERO. */
+int pic_push_deposit(pic_ctx* ctx, const pic_species* sp, int32_t nspecies, const void* EB,
+                     void* J, double dt, double omegaB0, double dx, uint32_t flags,
+                     void* stream);
+
+/* Metadomain::SynchronizeFields(Comm::J) + CommunicateFields(Comm::J)
+ * (metadomain_comm.cpp:408-562, 204-367): periodic ghost currents are added
+ * to their active images, then ghosts are refilled. buff is unused (kept for
+ * signature parity with the reference, which stages through it). */
+int pic_sync_currents(pic_ctx* ctx, void* J, void* buff, void* stream);
+
+/* srpic::CurrentsFilter (src/engines/srpic/currents.h:89-119):
+ * npasses x (buff <- J; DigitalFilter_kernel; CommunicateFields(J)),
+ * src/kernels/digital_filter.hpp:129-389, Cartesian. */
+int pic_filter_currents(pic_ctx* ctx, void* J, void* buff, int32_t npasses, void* stream);
+
+/* Metadomain::CommunicateFields for one field (periodic self-exchange,
+ * src/framework/domain/comm_nompi.hpp:44-63): ghosts of components [c0, c1)
+ * are filled from their active images. is_em selects em_stride vs cur_stride. */
+int pic_fill_ghosts(pic_ctx* ctx, void* field, int32_t is_em, int32_t c0, int32_t c1,
+                    void* stream);
+
+/* Metadomain::SortParticles (src/framework/domain/metadomain_sort.cpp:15-34)
+ * for one species: PIC_SORT_REMOVE_DEAD = Particles::RemoveDead
+ * (particles_sort.cpp:103-194), PIC_SORT_SPATIAL = Particles::SortSpatially
+ * (particles_sort.cpp:196-253) as a stable counting sort on the
+ * PositionToTileIndex key (src/global/utils/sorting.h:119-135). Synchronises
+ * the stream; writes the new npart (dead removed) to *npart_out. */
+int pic_sort(pic_ctx* ctx, pic_species* sp, uint32_t flags, int64_t* npart_out, void* stream);
+
+/* FP64 field energy: out[0] = sum E^2, out[1] = sum B^2 with the Minkowski
+ * weights of ReducedFields_kernel (src/kernels/reduced_stats.hpp:145-187).
+ * Synchronises the stream. */
+int pic_field_energy(pic_ctx* ctx, const void* EB, double dx, double* out, void* stream);
+
+/* Device error word: out[0] = particles with an invalid tag seen by the
+ * pusher, out[1] = alive particles found outside the grid by the sort.
+ * Synchronises the stream. reset != 0 clears the counters. */
+int pic_get_device_errors(pic_ctx* ctx, int64_t out[4], int32_t reset, void* stream);
+
+/* Phase timers, the counterpart of timer::Timers with blocking timers
+ * (src/global/utils/timer.h:51-148, phases of srpic.hpp:85-187): when enabled,
+ * pic_srpic_step records a CUDA event pair on its stream around every phase;
+ * pic_timers_read synchronises on the recorded events and returns the summed
+ * milliseconds and the number of intervals per phase. */
+#define PIC_PHASE_FIELDSOLVER 0    /* Faraday halves + Ampere + J->E (+ fused exchanges) */
+#define PIC_PHASE_PUSH_DEPOSIT 1   /* ParticlePusher + CurrentDeposit (fused) */
+#define PIC_PHASE_COMMUNICATIONS 2 /* J fold and ghost fill */
+#define PIC_PHASE_FILTERING 3      /* CurrentFiltering */
+#define PIC_PHASE_SORT 4           /* ParticleSort */
+#define PIC_PHASE_STEP 5           /* the whole step */
+#define PIC_NPHASES 6
+
+int pic_timers_enable(pic_ctx* ctx, int32_t on);
+int pic_timers_reset(pic_ctx* ctx);
+int pic_timers_read(pic_ctx* ctx, double ms[PIC_NPHASES], int64_t count[PIC_NPHASES]);
+/* record the start / end of one interval of `phase` on `stream` (no-ops when
+ * timers are disabled); used by the host engine */
+int pic_timer_mark(pic_ctx* ctx, int32_t phase, int32_t is_end, void* stream);
+
+/* The whole SR step of SRPICEngine::step_forward (srpic.hpp:65-188) for a
+ * periodic Cartesian domain, driven by the C++ host engine in this library:
+ * Faraday(1/2) + comm B, push + deposit of every species, J sync + comm,
+ * nfilter passes, Faraday(1/2) + comm B, Ampere + CurrentsAmpere + comm E,J,
+ * and a spatial sort of every species when sort_interval > 0 and
+ * step % sort_interval == 0. */
+typedef struct {
+  double  dt;
+  double  dx;
+  double  omegaB0;   /* scales.omegaB0 */
+  double  correction;/* algorithms.timestep.correction */
+  double  q0, B0, V0, ppc0;
+  int32_t nfilter;
+  int32_t sort_interval;
+  int32_t clear_interval;
+  int32_t fieldsolver_enabled;
+  int32_t deposit_enabled;
+  int32_t write_prev;
+} pic_step_params;
+
+int pic_srpic_step(pic_ctx* ctx, pic_species* sp, int32_t nspecies, void* EB, void* J,
+                   void* buff, const pic_step_params* prm, int64_t step, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ENTITY_PIC_H */

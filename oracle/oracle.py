@@ -1,0 +1,197 @@
+"""ctypes binding of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, as the checker. Arrays are CPU torch tensors in the same layout as the
+GPU path (see entity_gb300/inputs.py).
+"""
+import ctypes as C
+import os
+
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+class OrcGrid(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int), ("n1", C.c_int), ("n2", C.c_int), ("n3", C.c_int), ("ng", C.c_int),
+        ("em_s", C.c_int64 * 4), ("cur_s", C.c_int64 * 4),
+        ("periodic", C.c_int * 3), ("prtl_bc", (C.c_int * 2) * 3),
+    ]
+
+
+class OrcSpecies(C.Structure):
+    _fields_ = [
+        ("i1", C.c_void_p), ("i2", C.c_void_p), ("i3", C.c_void_p),
+        ("i1_prev", C.c_void_p), ("i2_prev", C.c_void_p), ("i3_prev", C.c_void_p),
+        ("dx1", C.c_void_p), ("dx2", C.c_void_p), ("dx3", C.c_void_p),
+        ("dx1_prev", C.c_void_p), ("dx2_prev", C.c_void_p), ("dx3_prev", C.c_void_p),
+        ("ux1", C.c_void_p), ("ux2", C.c_void_p), ("ux3", C.c_void_p),
+        ("weight", C.c_void_p), ("tag", C.c_void_p),
+        ("npart", C.c_int64), ("mass", C.c_float), ("charge", C.c_float), ("pusher", C.c_int),
+    ]
+
+
+_libs = {}
+
+
+def lib(real):
+    tag = "f32" if real == torch.float32 else "f64"
+    if tag not in _libs:
+        from . import build_oracle
+        paths = build_oracle.build()
+        L = C.CDLL(paths[tag])
+        V = C.c_void_p
+        G = C.POINTER(OrcGrid)
+        S = C.POINTER(OrcSpecies)
+        L.orc_push.restype = C.c_int64
+        L.orc_push.argtypes = [G, S, V, C.c_int, C.c_double, C.c_double, C.c_double]
+        L.orc_deposit.argtypes = [G, S, V, C.c_int, C.c_double, C.c_double]
+        L.orc_faraday.argtypes = [G, V, C.c_double, C.c_double, C.POINTER(C.c_double)]
+        L.orc_ampere.argtypes = [G, V, C.c_double, C.c_double]
+        L.orc_currents_ampere.argtypes = [G, V, V, C.c_double, C.c_double]
+        L.orc_filter_pass.argtypes = [G, V, V]
+        L.orc_fill_ghosts.argtypes = [G, V, C.c_int, C.c_int, C.c_int]
+        L.orc_sync_currents.argtypes = [G, V, V]
+        L.orc_sort.argtypes = [G, S, C.POINTER(C.c_int64)]
+        L.orc_remove_dead.restype = C.c_int64
+        L.orc_remove_dead.argtypes = [G, S]
+        L.orc_field_energy.argtypes = [G, V, C.c_double, C.POINTER(C.c_double)]
+        L.orc_kinetic_energy.restype = C.c_double
+        L.orc_kinetic_energy.argtypes = [S]
+        L.orc_max_threads.restype = C.c_int
+        L.orc_real_size.restype = C.c_int
+        _libs[tag] = L
+    return _libs[tag]
+
+
+def _p(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+class Oracle:
+    """The reference algorithm on the CPU for one grid (see srpic_oracle.h)."""
+
+    def __init__(self, g):
+        self.g = g
+        self.L = lib(g.real)
+        og = OrcGrid()
+        og.dim, og.ng = g.dim, g.ng
+        og.n1, og.n2 = g.n[0], g.n[1]
+        og.n3 = g.n[2] if g.dim == 3 else 1
+        s = g.strides()
+        for k in range(4):
+            og.em_s[k] = s[k]
+            og.cur_s[k] = s[k]
+        for d in range(3):
+            og.periodic[d] = int(g.periodic[d]) if d < g.dim else 0
+            og.prtl_bc[d][0] = g.prtl_bc[d][0]
+            og.prtl_bc[d][1] = g.prtl_bc[d][1]
+        self.og = og
+
+    def species(self, sp):
+        os_ = OrcSpecies()
+        os_.i1, os_.i2, os_.i3 = _p(sp.i[0]), _p(sp.i[1]), _p(sp.i[2])
+        os_.i1_prev, os_.i2_prev, os_.i3_prev = _p(sp.i_prev[0]), _p(sp.i_prev[1]), _p(sp.i_prev[2])
+        os_.dx1, os_.dx2, os_.dx3 = _p(sp.dx[0]), _p(sp.dx[1]), _p(sp.dx[2])
+        os_.dx1_prev, os_.dx2_prev, os_.dx3_prev = (_p(sp.dx_prev[0]), _p(sp.dx_prev[1]),
+                                                    _p(sp.dx_prev[2]))
+        os_.ux1, os_.ux2, os_.ux3 = _p(sp.u[0]), _p(sp.u[1]), _p(sp.u[2])
+        os_.weight, os_.tag = _p(sp.w), _p(sp.tag)
+        os_.npart, os_.mass, os_.charge, os_.pusher = sp.npart, sp.mass, sp.charge, sp.pusher
+        return os_
+
+    def push(self, sp, EB, dt, omegaB0, dx):
+        s = self.species(sp)
+        return self.L.orc_push(C.byref(self.og), C.byref(s), _p(EB), self.g.order, dt, omegaB0, dx)
+
+    def deposit(self, species, J, dt, dx, zero=True):
+        if zero:
+            J.zero_()
+        for sp in species:
+            s = self.species(sp)
+            self.L.orc_deposit(C.byref(self.og), C.byref(s), _p(J), self.g.order, dt, dx)
+
+    def faraday(self, EB, c1, c2, stencil=None):
+        st = None if stencil is None else (C.c_double * 9)(*stencil)
+        self.L.orc_faraday(C.byref(self.og), _p(EB), c1, c2, st)
+
+    def ampere(self, EB, c1, c2):
+        self.L.orc_ampere(C.byref(self.og), _p(EB), c1, c2)
+
+    def currents_ampere(self, EB, J, coeff, ppc0):
+        self.L.orc_currents_ampere(C.byref(self.og), _p(EB), _p(J), coeff, ppc0)
+
+    def filter_pass(self, J, buff):
+        self.L.orc_filter_pass(C.byref(self.og), _p(J), _p(buff))
+
+    def fill_ghosts(self, fld, is_em, c0, c1):
+        self.L.orc_fill_ghosts(C.byref(self.og), _p(fld), int(is_em), c0, c1)
+
+    def sync_currents(self, J, buff):
+        self.L.orc_sync_currents(C.byref(self.og), _p(J), _p(buff))
+
+    def sort(self, sp):
+        s = self.species(sp)
+        perm = torch.empty(max(sp.npart, 1), dtype=torch.int64)
+        self.L.orc_sort(C.byref(self.og), C.byref(s), C.cast(perm.data_ptr(), C.POINTER(C.c_int64)))
+        return perm[:sp.npart]
+
+    def remove_dead(self, sp):
+        s = self.species(sp)
+        n = self.L.orc_remove_dead(C.byref(self.og), C.byref(s))
+        sp.npart = n
+        return n
+
+    def field_energy(self, EB, dx):
+        out = (C.c_double * 2)()
+        self.L.orc_field_energy(C.byref(self.og), _p(EB), dx, out)
+        return out[0], out[1]
+
+    def kinetic_energy(self, sp):
+        s = self.species(sp)
+        return self.L.orc_kinetic_energy(C.byref(s))
+
+    # the SR step sequence of SRPICEngine::step_forward (srpic.hpp:65-188)
+    def step(self, species, EB, J, buff, prm, step, filter_passes=None):
+        g = self.g
+        R = g.real
+        t = lambda v: torch.tensor(v, dtype=R)
+        if step == 0:
+            self.fill_ghosts(EB, True, 0, 6)
+        dT = t(0.5) * t(prm.correction) * t(prm.dt)
+        dxm = torch.sqrt(t(prm.dx) * t(prm.dx))
+        c1 = dT / (dxm * dxm) if g.dim == 2 else dT / dxm
+        c2 = dT if g.dim == 2 else t(0.0)
+        if prm.fieldsolver_enabled:
+            self.faraday(EB, float(c1), float(c2))
+            self.fill_ghosts(EB, True, 3, 6)
+        for sp in species:
+            if sp.pusher != 0 and sp.npart > 0:
+                self.push(sp, EB, prm.dt, prm.omegaB0, prm.dx)
+        if prm.deposit_enabled:
+            self.deposit(species, J, prm.dt, prm.dx)
+            self.sync_currents(J, buff)
+            self.fill_ghosts(J, False, 0, 3)
+            for _ in range(prm.nfilter if filter_passes is None else filter_passes):
+                self.filter_pass(J, buff)
+                self.fill_ghosts(J, False, 0, 3)
+        if prm.fieldsolver_enabled:
+            self.faraday(EB, float(c1), float(c2))
+            self.fill_ghosts(EB, True, 3, 6)
+            dT1 = t(1.0) * t(prm.correction) * t(prm.dt)
+            a1 = dT1 / (dxm * dxm) if g.dim == 2 else dT1 / dxm
+            a2 = dT1 if g.dim == 2 else t(0.0)
+            self.ampere(EB, float(a1), float(a2))
+            if prm.deposit_enabled:
+                jc = -t(prm.dt) * t(prm.q0) / (t(prm.B0) * t(prm.V0))
+                self.currents_ampere(EB, J, float(jc), prm.ppc0)
+                self.fill_ghosts(EB, True, 0, 3)
+                self.fill_ghosts(J, False, 0, 3)
+            else:
+                self.fill_ghosts(EB, True, 0, 3)
+        for sp in species:
+            if prm.clear_interval > 0 and step % prm.clear_interval == 0 and step > 0:
+                self.remove_dead(sp)
+            if prm.sort_interval > 0 and step % prm.sort_interval == 0:
+                self.sort(sp)
