@@ -155,6 +155,8 @@ int run_pd(pic_ctx* c, const pic_species* sp, const void* EB, void* J, double dt
     a.pc.bc[d][1] = c->grid.prtl_bc[d][1];
   }
   a.pc.ng = c->grid.ng;
+  for (int d = 0; d < 3; ++d)
+    a.pc.ext[d] = d < c->grid.dim ? c->grid.n[d] + 2 * c->grid.ng : 1;
   a.EB    = em_view<real>(c, EB);
   a.J     = cur_view<real>(c, J);
   a.dt    = (real)dt;
@@ -316,6 +318,8 @@ int pic_faraday(pic_ctx* c, void* EB, double coeff1, double coeff2, const double
   if (st) {
     for (int k = 0; k < 9; ++k) yee = yee && st[k] == 0.0;
   }
+  // the extended stencil reads two cells beyond the active range
+  if (!yee && c->grid.ng < 2) return PIC_ERR_ARG;
   if (is_f64(c)) {
     pic::Stencil<double> s{};
     if (st) s = { st[0], st[1], st[2], st[3], st[4], st[5], st[6], st[7], st[8] };

@@ -412,10 +412,20 @@ __device__ __forceinline__ void move_and_bound(Prtl<real>& q, bool massive, real
 // current deposit of one particle: src/kernels/currents_deposit.hpp:108-761
 // `add(i, j, k, c, v)` accumulates v into J at ghost-inclusive (i, j, k).
 // ---------------------------------------------------------------------------
+// Returns false, touching nothing, when the particle's stencil would reach
+// outside the ghost-inclusive extents `ext` (possible only for moves longer
+// than the ghost layers allow, i.e. a time step beyond the CFL limit).
 template <int D, int O, typename real, typename Add>
-__device__ __forceinline__ void deposit_particle(const Prtl<real>& q, real weight, real charge,
-                                                 real inv_dt, real dx, int ng, Add&& add) {
+__device__ __forceinline__ bool deposit_particle(const Prtl<real>& q, real weight, real charge,
+                                                 real inv_dt, real dx, int ng, const int* ext,
+                                                 Add&& add) {
   const real ONE = 1, HALF = 0.5, INV_2 = 0.5, ZERO = 0;
+  if constexpr (O == 0) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      if (min(q.ip[a], q.i[a]) + ng < 0 || max(q.ip[a], q.i[a]) + ng + 1 >= ext[a]) return false;
+    }
+  }
   real       vp[3];
   vp[0] = q.u[0] / dx;
   vp[1] = q.u[1] / dx;
@@ -493,6 +503,7 @@ __device__ __forceinline__ void deposit_particle(const Prtl<real>& q, real weigh
 #pragma unroll
     for (int a = 0; a < D; ++a) {
       for_deposit<O>(q.ip[a], (real)q.dxp[a], q.i[a], (real)q.dx[a], imin[a], imax[a], iS[a], fS[a]);
+      if (imin[a] + ng < 0 || imax[a] + ng >= ext[a]) return false;
     }
     const real THIRD = K<real>::THIRD;
     const real Q     = coeff * inv_dt;
@@ -596,6 +607,16 @@ __device__ __forceinline__ void deposit_particle(const Prtl<real>& q, real weigh
       }
     }
   }
+  return true;
+}
+
+// true when the cell of every simulated axis lies in [0, n)
+template <int D>
+__device__ __forceinline__ bool cells_in_grid(const int* i, const int* n) {
+  bool ok = true;
+#pragma unroll
+  for (int a = 0; a < D; ++a) ok = ok && (i[a] >= 0) && (i[a] < n[a]);
+  return ok;
 }
 
 }  // namespace pic

@@ -12,6 +12,7 @@ struct PushConsts {
   int n[3];
   int bc[3][2];
   int ng;
+  int ext[3];  // ghost-inclusive extents (1 along an unsimulated axis)
 };
 
 // raw species pointers for a kernel (real arrays typed by the kernel)
@@ -32,7 +33,7 @@ struct Strides {
 };
 
 // device error counters (index meaning documented in entity_pic.h)
-enum ErrIdx { ERR_BAD_TAG = 0, ERR_OUT_OF_GRID = 1, ERR_RESERVED2 = 2, ERR_RESERVED3 = 3 };
+enum ErrIdx { ERR_BAD_TAG = 0, ERR_OUT_OF_GRID = 1, ERR_STENCIL_OUT = 2, ERR_RESERVED3 = 3 };
 
 // process-wide count of kernels this library has launched
 void note_launch();

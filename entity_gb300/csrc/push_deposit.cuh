@@ -53,6 +53,11 @@ __global__ void __launch_bounds__(256) k_push_deposit(PDArgs<real> a) {
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) q.u[d] = ux[d][p];
+    if (!cells_in_grid<D>(q.i, a.pc.n)) {
+      // a cell outside the grid is invalid input; report it, touch nothing
+      atomicAdd(a.err + ERR_OUT_OF_GRID, 1ull);
+      continue;
+    }
     if constexpr (MODE == MODE_DEPOSIT) {
 #pragma unroll
       for (int d = 0; d < D; ++d) {
@@ -101,10 +106,11 @@ __global__ void __launch_bounds__(256) k_push_deposit(PDArgs<real> a) {
     if constexpr (MODE != MODE_PUSH) {
       if (q.tag == PIC_TAG_DEAD) continue;
       const FieldView<real>& J = a.J;
-      deposit_particle<D, O, real>(q, w[p], a.charge, a.inv_dt, a.dx, a.pc.ng,
-                                   [&](int i, int j, int k, int c, real v) {
-                                     atomicAdd(J.p + J.idx(i, j, k, c), v);
-                                   });
+      const bool ok = deposit_particle<D, O, real>(q, w[p], a.charge, a.inv_dt, a.dx, a.pc.ng,
+                                                   a.pc.ext, [&](int i, int j, int k, int c, real v) {
+                                                     atomicAdd(J.p + J.idx(i, j, k, c), v);
+                                                   });
+      if (!ok) atomicAdd(a.err + ERR_STENCIL_OUT, 1ull);
     }
   }
 }

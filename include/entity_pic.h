@@ -198,7 +198,10 @@ int pic_sort(pic_ctx* ctx, pic_species* sp, uint32_t flags, int64_t* npart_out, 
 int pic_field_energy(pic_ctx* ctx, const void* EB, double dx, double* out, void* stream);
 
 /* Device error word: out[0] = particles with an invalid tag seen by the
- * pusher, out[1] = alive particles found outside the grid by the sort.
+ * pusher, out[1] = alive particles whose cell lies outside the grid (skipped
+ * by the pusher, reported by the sort), out[2] = particles whose deposit
+ * stencil would leave the ghost layers (a step beyond the CFL limit; their
+ * current is not deposited).
  * Synchronises the stream. reset != 0 clears the counters. */
 int pic_get_device_errors(pic_ctx* ctx, int64_t out[4], int32_t reset, void* stream);
 
