@@ -82,11 +82,11 @@ def make_setup(w, device, n=None):
     return g, EB, J, buff, sp
 
 
-def step_prm(g, w, sort_interval):
+def step_prm(g, w, sort_interval, sort_tiled=True):
     from entity_gb300.sim import step_params
     return step_params(g, cfl=w["cfl"], ppc0=w["ppc0"], skindepth0=w["skindepth0"],
                        larmor0=w["larmor0"], nfilter=w["nfilter"], sort_interval=sort_interval,
-                       write_prev=False)
+                       write_prev=False, sort_tiled=sort_tiled)
 
 
 class ClockSampler:
@@ -196,8 +196,8 @@ def run_ours(args, w):
     from entity_gb300.sim import Context
     lib = abi.load()
 
-    g, EB, J, buff, sp = make_setup(w, "cuda")
-    prm = step_prm(g, w, args.sort_interval)
+    g, EB, J, buff, sp = make_setup(w, "cuda", n=args.cells)
+    prm = step_prm(g, w, args.sort_interval, sort_tiled=not args.reference_sort_key)
     ctx = Context(g)
     npart = sum(s.npart for s in sp)
     torch.cuda.synchronize()
@@ -290,6 +290,7 @@ def run_ours(args, w):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": w["name"], "cells": g.ncells(), "particles_per_gpu": npart,
                    "sort_interval": args.sort_interval,
+                   "sort_key": "reference cell key" if args.reference_sort_key else "tile-major",
                    "l2": "inputs larger than L2 (particle state > 10 GB per step)",
                    "parallelism": f"replicas x{world}"},
         "ns_per_particle_step": 1e9 / (value / world),
@@ -314,13 +315,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="turb3d", choices=sorted(WORKLOADS))
-    ap.add_argument("--sort-interval", type=int, default=5)
+    ap.add_argument("--sort-interval", type=int, default=4)
+    ap.add_argument("--reference-sort-key", action="store_true",
+                    help="sort by the reference's i1-major cell key (untiled push/deposit)")
+    ap.add_argument("--cells", type=int, nargs="+", default=None,
+                    help="override the grid (smaller cases for profiling)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
+    if args.cells is not None:
+        c = list(args.cells) + [1] * (3 - len(args.cells))
+        args.cells = tuple(c)
     if args.impl == "reference":
         run_reference(args, w)
     else:

@@ -36,6 +36,7 @@ PIC_PD_NO_ZERO = 2
 PIC_SORT_REMOVE_DEAD = 1
 PIC_SORT_SKIP_PREV = 2
 PIC_SORT_SPATIAL = 4
+PIC_SORT_TILED = 8
 
 
 class PicGrid(C.Structure):
@@ -77,7 +78,7 @@ class PicStepParams(C.Structure):
         ("q0", C.c_double), ("B0", C.c_double), ("V0", C.c_double), ("ppc0", C.c_double),
         ("nfilter", C.c_int32), ("sort_interval", C.c_int32), ("clear_interval", C.c_int32),
         ("fieldsolver_enabled", C.c_int32), ("deposit_enabled", C.c_int32),
-        ("write_prev", C.c_int32),
+        ("write_prev", C.c_int32), ("sort_tiled", C.c_int32),
     ]
 
 
@@ -90,6 +91,7 @@ SIGNATURES = {
     "pic_create": (C.c_int, [C.POINTER(PicGrid), C.POINTER(_VP)]),
     "pic_destroy": (C.c_int, [_VP]),
     "pic_get_grid": (C.c_int, [_VP, C.POINTER(PicGrid)]),
+    "pic_tile_shape": (C.c_int, [_VP, C.POINTER(C.c_int32)]),
     "pic_faraday": (C.c_int, [_VP, _VP, C.c_double, C.c_double, C.POINTER(C.c_double), _VP]),
     "pic_ampere": (C.c_int, [_VP, _VP, C.c_double, C.c_double, _VP]),
     "pic_currents_ampere": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_double, _VP]),

@@ -4,6 +4,7 @@
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 #include <utility>
 #include <vector>
 #include <cstring>
@@ -11,10 +12,48 @@
 
 #include "../../include/entity_pic.h"
 #include "fields.cuh"
-#include "push_deposit.cuh"
+#include "push_deposit_tiled.cuh"
 #include "sort.cuh"
 
+namespace pic {
+namespace {
+template <int D, typename real, int O>
+void shape_of(int out[3]) {
+  out[0] = TileShape<D, real, O>::X;
+  out[1] = TileShape<D, real, O>::Y;
+  out[2] = D == 3 ? TileShape<D, real, O>::Z : 1;
+}
+template <int D, typename real>
+void shape_by_order(int order, int out[3]) {
+  switch (order) {
+    case 0: shape_of<D, real, 0>(out); break;
+    case 1: shape_of<D, real, 1>(out); break;
+    case 2: shape_of<D, real, 2>(out); break;
+    default: shape_of<D, real, 3>(out); break;
+  }
+}
+}  // namespace
+void tile_shape(int dim, int real_bytes, int order, int out[3]) {
+  if (dim == 3 && real_bytes == 4) shape_by_order<3, float>(order, out);
+  else if (dim == 3)               shape_by_order<3, double>(order, out);
+  else if (real_bytes == 4)        shape_by_order<2, float>(order, out);
+  else                             shape_by_order<2, double>(order, out);
+}
+}  // namespace pic
+
+// tile-major binning of one species, valid from a PIC_SORT_TILED sort until
+// the species' particle count changes or it is sorted with another key
+struct SpeciesBins {
+  int32_t  index      = 0;
+  int64_t  nalive     = 0;  // particles [0, nalive) are binned by tile
+  int64_t  npart      = 0;  // npart right after the sort
+  int32_t* tile_start = nullptr;
+  int      ntiles     = 0;
+  bool     valid      = false;
+};
+
 struct pic_ctx {
+  std::vector<SpeciesBins> bins;
   pic_grid             grid;
   unsigned long long*  d_err     = nullptr;  // 4 counters
   double*              d_energy  = nullptr;  // 2
@@ -174,6 +213,99 @@ int run_pd(pic_ctx* c, const pic_species* sp, const void* EB, void* J, double dt
   return cuda_status(pd_dispatch<real>(c, a, mode, photon, s));
 }
 
+SpeciesBins* find_bins(pic_ctx* c, int index, bool create) {
+  for (auto& b : c->bins)
+    if (b.index == index) return &b;
+  if (!create) return nullptr;
+  c->bins.emplace_back();
+  c->bins.back().index = index;
+  return &c->bins.back();
+}
+
+void ntiles_of(const pic_ctx* c, int nt[3], int ts[3]) {
+  pic::tile_shape(c->grid.dim, c->grid.real_bytes, c->grid.order, ts);
+  for (int d = 0; d < 3; ++d) {
+    const int n = d < c->grid.dim ? c->grid.n[d] : 1;
+    nt[d]       = (n + ts[d] - 1) / ts[d];
+  }
+}
+
+// a copy of `sp` whose arrays start at particle `first`
+pic_species species_tail(const pic_species& sp, int64_t first, int real_bytes) {
+  pic_species t = sp;
+  auto adv      = [&](auto*& p, size_t esz) {
+    using P = std::remove_reference_t<decltype(p)>;
+    if (p) p = (P)((char*)p + esz * first);
+  };
+  adv(t.i1, 4);
+  adv(t.i2, 4);
+  adv(t.i3, 4);
+  adv(t.i1_prev, 4);
+  adv(t.i2_prev, 4);
+  adv(t.i3_prev, 4);
+  adv(t.dx1, 4);
+  adv(t.dx2, 4);
+  adv(t.dx3, 4);
+  adv(t.dx1_prev, 4);
+  adv(t.dx2_prev, 4);
+  adv(t.dx3_prev, 4);
+  adv(t.ux1, real_bytes);
+  adv(t.ux2, real_bytes);
+  adv(t.ux3, real_bytes);
+  adv(t.weight, real_bytes);
+  adv(t.tag, 2);
+  t.npart    = sp.npart - first;
+  t.maxnpart = 0;
+  return t;
+}
+
+template <typename real>
+int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void* EB, void* J,
+              double dt, double omegaB0, double dx, bool write_prev, cudaStream_t s) {
+  pic::TiledArgs<real> a;
+  a.nsp = (int)sps.size();
+  for (int k = 0; k < a.nsp; ++k) {
+    const pic_species* sp = sps[k];
+    a.s[k].sp             = sptrs(sp);
+    a.s[k].tile_start     = find_bins(c, sp->index, false)->tile_start;
+    const float qm        = sp->charge / sp->mass;
+    a.s[k].ndth           = (real)0.5 * (real)qm * (real)omegaB0 * (real)dt;
+    a.s[k].charge         = (real)sp->charge;
+    a.s[k].vay            = sp->pusher == PIC_PUSHER_VAY;
+  }
+  int ts[3];
+  ntiles_of(c, a.ntiles, ts);
+  for (int d = 0; d < 3; ++d) {
+    a.pc.n[d]     = c->grid.n[d];
+    a.pc.bc[d][0] = c->grid.prtl_bc[d][0];
+    a.pc.bc[d][1] = c->grid.prtl_bc[d][1];
+    a.pc.ext[d]   = d < c->grid.dim ? c->grid.n[d] + 2 * c->grid.ng : 1;
+    a.periodic[d] = d < c->grid.dim ? c->grid.fld_periodic[d] : 0;
+  }
+  a.pc.ng      = c->grid.ng;
+  a.EB         = em_view<real>(c, EB);
+  a.J          = cur_view<real>(c, J);
+  a.dt         = (real)dt;
+  a.dx         = (real)dx;
+  a.inv_dt     = (real)1 / (real)dt;
+  a.write_prev = write_prev ? 1 : 0;
+  a.err        = c->d_err;
+  const int D = c->grid.dim, O = c->grid.order;
+  cudaError_t e = cudaErrorInvalidValue;
+#define PIC_TD(DD, OO) \
+  if (D == DD && O == OO) e = pic::launch_push_deposit_tiled<DD, OO, real>(a, s);
+  PIC_TD(2, 0)
+  PIC_TD(2, 1)
+  PIC_TD(2, 2)
+  PIC_TD(2, 3)
+  PIC_TD(3, 0)
+  PIC_TD(3, 1)
+  PIC_TD(3, 2)
+  PIC_TD(3, 3)
+#undef PIC_TD
+  return cuda_status(e);
+}
+
 template <typename real>
 int zero_J(pic_ctx* c, void* J, cudaStream_t s) {
   return cuda_status(pic::launch_zero3<real>(ginfo(c), cur_view<real>(c, J), s));
@@ -252,6 +384,7 @@ int pic_destroy(pic_ctx* c) {
   cudaDeviceSynchronize();
   pic_timers_reset(c);
   for (auto e : c->event_pool) cudaEventDestroy(e);
+  for (auto& b : c->bins) cudaFree(b.tile_start);
   cudaFree(c->d_err);
   cudaFree(c->d_energy);
   if (c->sort_buf) cudaFree(c->sort_buf);
@@ -309,6 +442,14 @@ int pic_timers_read(pic_ctx* c, double ms[PIC_NPHASES], int64_t count[PIC_NPHASE
 int pic_get_grid(const pic_ctx* c, pic_grid* out) {
   if (!c || !out) return PIC_ERR_ARG;
   *out = c->grid;
+  return PIC_OK;
+}
+
+int pic_tile_shape(const pic_ctx* c, int32_t out[3]) {
+  if (!c || !out) return PIC_ERR_ARG;
+  int ts[3];
+  pic::tile_shape(c->grid.dim, c->grid.real_bytes, c->grid.order, ts);
+  for (int d = 0; d < 3; ++d) out[d] = ts[d];
   return PIC_OK;
 }
 
@@ -417,9 +558,32 @@ int pic_push_deposit(pic_ctx* c, const pic_species* sp, int32_t nspecies, const 
     st = is_f64(c) ? zero_J<double>(c, J, strm(stream)) : zero_J<float>(c, J, strm(stream));
     if (st != PIC_OK) return st;
   }
+  // species with a valid tile binning (PIC_SORT_TILED) go through the tiled
+  // kernel together; the rest, and any particles beyond a binned prefix,
+  // through the per-particle kernel
+  std::vector<const pic_species*> tiled;
+  std::vector<pic_species>        rest;
   for (int k = 0; k < nspecies; ++k) {
     const pic_species* s = sp + k;
     if (s->pusher == PIC_PUSHER_NONE || s->npart == 0) continue;
+    const SpeciesBins* b = find_bins(c, s->index, false);
+    const bool eligible  = b && b->valid && b->npart == s->npart &&
+                          (s->pusher == PIC_PUSHER_BORIS || s->pusher == PIC_PUSHER_VAY) &&
+                          (int)tiled.size() < pic::kMaxTiledSpecies;
+    if (eligible) {
+      tiled.push_back(s);
+      if (b->nalive < s->npart) rest.push_back(species_tail(*s, b->nalive, c->grid.real_bytes));
+    } else {
+      rest.push_back(*s);
+    }
+  }
+  if (!tiled.empty()) {
+    st = is_f64(c) ? run_tiled<double>(c, tiled, EB, J, dt, omegaB0, dx, write_prev, strm(stream))
+                   : run_tiled<float>(c, tiled, EB, J, dt, omegaB0, dx, write_prev, strm(stream));
+    if (st != PIC_OK) return st;
+  }
+  for (const pic_species& rs : rest) {
+    const pic_species* s = &rs;
     // a species that moves but carries no charge is pushed only
     const int mode = (s->charge == 0.0f) ? pic::MODE_PUSH : pic::MODE_FUSED;
     if (mode == pic::MODE_PUSH && !write_prev) {
@@ -505,8 +669,18 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
   if (np == 0 || (!remove_dead && !spatial)) return PIC_OK;
 
   const pic_grid& g     = c->grid;
-  const int64_t   cells = spatial ? (int64_t)g.n[0] * g.n[1] * (g.dim == 3 ? g.n[2] : 1) : 1;
-  const int64_t   nbins = cells + 1;  // + dead bin
+  const bool      tiled = spatial && (flags & PIC_SORT_TILED) != 0;
+  int             nt[3] = { 1, 1, 1 }, ts[3] = { 1, 1, 1 };
+  if (tiled) ntiles_of(c, nt, ts);
+  const int64_t   ntiles = (int64_t)nt[0] * nt[1] * nt[2];
+  const int64_t   tcells = (int64_t)ts[0] * ts[1] * ts[2];
+  const int64_t   cells  = !spatial ? 1
+                           : tiled  ? ntiles * tcells
+                                    : (int64_t)g.n[0] * g.n[1] * (g.dim == 3 ? g.n[2] : 1);
+  const int64_t   nbins  = cells + 1;  // + dead bin
+  if (cells >= ((int64_t)1 << 31) - 2) return PIC_ERR_UNSUPPORTED;
+  // any sort moves particles: the previous tile binning no longer holds
+  if (SpeciesBins* b = find_bins(c, sp->index, false)) b->valid = false;
   // scratch layout (8-byte aligned pieces)
   auto          al   = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t  b_key = al(4 * np), b_rank = al(4 * np), b_dead = al(np), b_drank = al(8 * np);
@@ -535,6 +709,11 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
   a.n[1] = g.n[1];
   a.n[2] = g.n[2];
   a.spatial = spatial ? 1 : 0;
+  a.tiled   = tiled ? 1 : 0;
+  for (int d = 0; d < 3; ++d) {
+    a.tile[d]   = ts[d];
+    a.ntiles[d] = nt[d];
+  }
   a.dead_bin = (int32_t)cells;
   a.key = (int32_t*)base;
   base += b_key;
@@ -603,6 +782,21 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
     newn = np - n_dead;
     if ((e = pic::set_tags(sp->tag, 0, newn, PIC_TAG_ALIVE, s)) != cudaSuccess) return PIC_ERR_CUDA;
     if ((e = pic::set_tags(sp->tag, newn, np, PIC_TAG_DEAD, s)) != cudaSuccess) return PIC_ERR_CUDA;
+  }
+  if (tiled) {
+    SpeciesBins* b = find_bins(c, sp->index, true);
+    if (b->ntiles != (int)ntiles || !b->tile_start) {
+      if (b->tile_start) cudaFree(b->tile_start);
+      b->tile_start = nullptr;
+      if (cudaMalloc((void**)&b->tile_start, sizeof(int32_t) * (ntiles + 1)) != cudaSuccess)
+        return PIC_ERR_NOMEM;
+      b->ntiles = (int)ntiles;
+    }
+    if ((e = pic::tile_offsets(a.off, tcells, (int)ntiles, b->tile_start, s)) != cudaSuccess)
+      return PIC_ERR_CUDA;
+    b->nalive = np - n_dead;
+    b->npart  = newn;
+    b->valid  = true;
   }
   unsigned long long h_err[4];
   if (cudaMemcpyAsync(h_err, c->d_err, sizeof(h_err), cudaMemcpyDeviceToHost, s) != cudaSuccess)

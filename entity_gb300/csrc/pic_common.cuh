@@ -167,11 +167,23 @@ struct FieldView {
   }
 };
 
+// a window of a field staged in shared memory: ghost-inclusive index g maps
+// to window index g - off along every axis; 32-bit strides
+template <typename real>
+struct SmemView {
+  const real* p;
+  int         off0, off1, off2;
+  int         s1, s2, s3;
+  __device__ __forceinline__ real ld(int i, int j, int k, int c) const {
+    return p[(i - off0) + (j - off1) * s1 + (k - off2) * s2 + c * s3];
+  }
+};
+
 // ---------------------------------------------------------------------------
-// interpolation: src/kernels/pushers/sr.hpp:851-1369
+// interpolation: src/kernels/pushers/sr.hpp:851-1369 (V = FieldView or SmemView)
 // ---------------------------------------------------------------------------
-template <int D, typename real>
-__device__ __forceinline__ void interp_zigzag(const FieldView<real>& EB, const int* ic,
+template <int D, typename real, typename V>
+__device__ __forceinline__ void interp_zigzag(const V& EB, const int* ic,
                                               const real* d_, real* e0, real* b0) {
   const real ONE = 1, HALF = 0.5;
   int        ind[3];
@@ -232,8 +244,8 @@ __device__ __forceinline__ void interp_zigzag(const FieldView<real>& EB, const i
   }
 }
 
-template <int D, int O, typename real>
-__device__ __forceinline__ void interp_shape(const FieldView<real>& EB, const int* ic,
+template <int D, int O, typename real, typename V>
+__device__ __forceinline__ void interp_shape(const V& EB, const int* ic,
                                              const real* dc, real* e0, real* b0) {
   // sr.hpp:1151-1369; running sums as fma(S, EB, c)
   int  pmin[3] = { 0, 0, 0 }, dmin[3] = { 0, 0, 0 };
@@ -349,6 +361,7 @@ struct Prtl {
   float dxp[3];
   real  u[3];
   short tag;
+  int   wrap[3];  // periodic shift applied to i and ip by the boundary step
 };
 
 // positionPush (Cartesian) + boundaryConditions: sr.hpp:526-572, 659-814.
@@ -363,7 +376,8 @@ __device__ __forceinline__ void move_and_bound(Prtl<real>& q, bool massive, real
             : (dt / sqrt(q.u[0] * q.u[0] + q.u[1] * q.u[1] + q.u[2] * q.u[2]));
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    q.ip[a]  = q.i[a];
+    q.ip[a]   = q.i[a];
+    q.wrap[a] = 0;
     q.dxp[a] = q.dx[a];
     q.dx[a] += (q.u[a] / dx) * dt_inv_energy;
     q.i[a] += (int)(q.dx[a] >= ONE) - (int)(q.dx[a] < ZERO);
@@ -378,6 +392,7 @@ __device__ __forceinline__ void move_and_bound(Prtl<real>& q, bool massive, real
       if (bc == PIC_BC_PERIODIC) {
         q.i[a] += pc.n[a];
         q.ip[a] += pc.n[a];
+        q.wrap[a] = pc.n[a];
       } else if (bc == PIC_BC_ABSORB) {
         q.tag = PIC_TAG_DEAD;
       } else if (bc == PIC_BC_REFLECT) {
@@ -393,6 +408,7 @@ __device__ __forceinline__ void move_and_bound(Prtl<real>& q, bool massive, real
       if (bc == PIC_BC_PERIODIC) {
         q.i[a] -= pc.n[a];
         q.ip[a] -= pc.n[a];
+        q.wrap[a] = -pc.n[a];
       } else if (bc == PIC_BC_ABSORB) {
         q.tag = PIC_TAG_DEAD;
       } else if (bc == PIC_BC_REFLECT) {
@@ -414,16 +430,19 @@ __device__ __forceinline__ void move_and_bound(Prtl<real>& q, bool massive, real
 // ---------------------------------------------------------------------------
 // Returns false, touching nothing, when the particle's stencil would reach
 // outside the ghost-inclusive extents `ext` (possible only for moves longer
-// than the ghost layers allow, i.e. a time step beyond the CFL limit).
+// than the ghost layers allow, i.e. a time step beyond the CFL limit);
+// ext == nullptr skips the check (the caller guarantees the window).
 template <int D, int O, typename real, typename Add>
 __device__ __forceinline__ bool deposit_particle(const Prtl<real>& q, real weight, real charge,
                                                  real inv_dt, real dx, int ng, const int* ext,
                                                  Add&& add) {
   const real ONE = 1, HALF = 0.5, INV_2 = 0.5, ZERO = 0;
   if constexpr (O == 0) {
+    if (ext) {
 #pragma unroll
-    for (int a = 0; a < D; ++a) {
-      if (min(q.ip[a], q.i[a]) + ng < 0 || max(q.ip[a], q.i[a]) + ng + 1 >= ext[a]) return false;
+      for (int a = 0; a < D; ++a) {
+        if (min(q.ip[a], q.i[a]) + ng < 0 || max(q.ip[a], q.i[a]) + ng + 1 >= ext[a]) return false;
+      }
     }
   }
   real       vp[3];
@@ -503,7 +522,7 @@ __device__ __forceinline__ bool deposit_particle(const Prtl<real>& q, real weigh
 #pragma unroll
     for (int a = 0; a < D; ++a) {
       for_deposit<O>(q.ip[a], (real)q.dxp[a], q.i[a], (real)q.dx[a], imin[a], imax[a], iS[a], fS[a]);
-      if (imin[a] + ng < 0 || imax[a] + ng >= ext[a]) return false;
+      if (ext && (imin[a] + ng < 0 || imax[a] + ng >= ext[a])) return false;
     }
     const real THIRD = K<real>::THIRD;
     const real Q     = coeff * inv_dt;

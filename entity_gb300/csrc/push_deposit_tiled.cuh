@@ -1,0 +1,384 @@
+// Tiled fused push + deposit: one CTA per tile of cells.
+//
+// The species' particles are stored tile-major (PIC_SORT_TILED), so the
+// particles of a tile are one contiguous range per species and are read and
+// written back fully coalesced. The CTA
+//   1. stages the E/B window of its tile (tile + interpolation halo + a drift
+//      margin of M cells) in shared memory,
+//   2. pushes every particle of the tile (all species) gathering E/B from
+//      shared memory and depositing its current into a shared-memory J window
+//      (tile + deposit halo + margin),
+//   3. adds the J window to global J once, wrapping periodic images onto
+//      their active cells (the fold SynchronizeFields performs in the
+//      reference, src/framework/domain/metadomain_comm.cpp:408-562).
+//
+// Accumulation in the J window: fixed point split over 32-bit words.
+// Only 32-bit integer shared-memory atomics are native on this GPU, and they
+// combine lanes that hit the same address; float, double and 64-bit integer
+// shared atomics serialise such lanes, and cell-sorted particles make these
+// collisions the common case. Each tile scales contributions by a power of
+// two 2^s so that |v 2^s| < 2^b, converts to a 64-bit integer (exact up to
+// the quantisation 2^-s) and adds it as 32-bit words: a 12-bit low word and a
+// signed high word (float), or three 16-bit words and a signed top word
+// (double). With N particles in the tile no cell takes more than N additions
+// per component, so b = 43 - log2 N (float; 29 bits at 16k particles) or
+// b = 62 - log2 N (double) overflows neither a word nor the 64-bit total.
+// The tile's sum is exact and
+// independent of the order of the additions; each cell is rounded to real
+// once, at the flush. A tile denser than the words allow (N > 2^20 in float,
+// 2^16 in double) accumulates in real_t atomics instead.
+//
+// A particle that has drifted more than M cells outside its tile since the
+// last tiled sort gathers E/B from global memory and deposits with global
+// atomics instead, so results never depend on the sort interval.
+// Arithmetic per particle is the same code as the untiled kernel.
+#pragma once
+
+#include <type_traits>
+
+#include "push_deposit.cuh"
+
+namespace pic {
+
+constexpr int kMaxTiledSpecies = 4;
+constexpr int kDriftMargin     = 1;
+
+// the J-window accumulator words of one precision (see the header)
+template <typename real>
+struct FixedAcc;
+template <>
+struct FixedAcc<float> {
+  static constexpr int     WORDS = 2;
+  static constexpr int64_t NMAX  = 1 << 20;  // low-word sums stay below 2^32
+  __device__ static int bits(int64_t n) { return 43 - (n > 1 ? 64 - __clzll(n - 1) : 0); }
+  __device__ static void add(unsigned* w, int plane, float v, float scale) {
+    const long long X = __float2ll_rn(v * scale);
+    atomicAdd(w, (unsigned)(X & 0xFFF));
+    atomicAdd(w + plane, (unsigned)(int)(X >> 12));
+  }
+  __device__ static bool nonzero(const unsigned* w, int plane) { return (w[0] | w[plane]) != 0u; }
+  __device__ static float value(const unsigned* w, int plane, float unscale) {
+    const unsigned long long t = ((unsigned long long)(long long)(int)w[plane] << 12) + w[0];
+    return __ll2float_rn((long long)t) * unscale;
+  }
+};
+template <>
+struct FixedAcc<double> {
+  static constexpr int     WORDS = 4;
+  static constexpr int64_t NMAX  = 1 << 16;  // 16-bit word sums stay below 2^32
+  // the 64-bit total of N additions must not overflow either
+  __device__ static int bits(int64_t n) { return 62 - (n > 1 ? 64 - __clzll(n - 1) : 0); }
+  __device__ static void add(unsigned* w, int plane, double v, double scale) {
+    const long long X = __double2ll_rn(v * scale);
+    atomicAdd(w, (unsigned)(X & 0xFFFF));
+    atomicAdd(w + plane, (unsigned)((X >> 16) & 0xFFFF));
+    atomicAdd(w + 2 * plane, (unsigned)((X >> 32) & 0xFFFF));
+    atomicAdd(w + 3 * plane, (unsigned)(int)(X >> 48));
+  }
+  __device__ static bool nonzero(const unsigned* w, int plane) {
+    return (w[0] | w[plane] | w[2 * plane] | w[3 * plane]) != 0u;
+  }
+  __device__ static double value(const unsigned* w, int plane, double unscale) {
+    const unsigned long long t = ((unsigned long long)(long long)(int)w[3 * plane] << 48) +
+                                 ((unsigned long long)w[2 * plane] << 32) +
+                                 ((unsigned long long)w[plane] << 16) + w[0];
+    return __ll2double_rn((long long)t) * unscale;
+  }
+};
+
+// tile shape per (dimension, precision, order): the shared-memory windows
+// must fit one CTA's 227 KB
+template <int D, typename real, int O>
+struct TileShape {
+  static constexpr int X = 32, Y = 32, Z = 1, NT = 256;  // 2D
+};
+template <int O>
+struct TileShape<3, float, O> {
+  static constexpr int X = 16, Y = 8, Z = (O == 3 ? 4 : 8), NT = 512;
+};
+template <int O>
+struct TileShape<3, double, O> {
+  static constexpr int X = 8, Y = 8, Z = 4, NT = 256;
+};
+
+// window halos (cells below / above the tile) of the interpolation and the
+// deposit stencils at order O, plus the drift margin
+template <int O>
+struct Halo {
+  static constexpr int E_LO = (O == 3 ? 2 : 1) + kDriftMargin;
+  static constexpr int E_HI = (O >= 2 ? 2 : 1) + kDriftMargin;
+  static constexpr int J_LO = (O >= 2 ? 2 : 1) + kDriftMargin;
+  static constexpr int J_HI = (O >= 2 ? 3 : 2) + kDriftMargin;
+};
+
+template <typename real>
+struct TiledSpecies {
+  SpeciesPtrs    sp;
+  const int32_t* tile_start;  // ntiles + 1 offsets into the particle arrays
+  real           ndth, charge;
+  int            vay;
+};
+
+template <typename real>
+struct TiledArgs {
+  TiledSpecies<real> s[kMaxTiledSpecies];
+  int                nsp;
+  PushConsts         pc;
+  int                periodic[3];
+  int                ntiles[3];
+  FieldView<real>    EB;
+  FieldView<real>    J;
+  real               dt, dx, inv_dt;
+  int                write_prev;
+  unsigned long long* err;
+};
+
+template <int D, int O, typename real>
+struct TiledGeom {
+  using TS                = TileShape<D, real, O>;
+  static constexpr int TX = TS::X, TY = TS::Y, TZ = (D == 3 ? TS::Z : 1);
+  static constexpr int NT = TS::NT;
+  using H                 = Halo<O>;
+  static constexpr int WE0 = TX + H::E_LO + H::E_HI;
+  static constexpr int WE1 = TY + H::E_LO + H::E_HI;
+  static constexpr int WE2 = D == 3 ? TZ + H::E_LO + H::E_HI : 1;
+  static constexpr int WJ0 = TX + H::J_LO + H::J_HI;
+  static constexpr int WJ1 = TY + H::J_LO + H::J_HI;
+  static constexpr int WJ2 = D == 3 ? TZ + H::J_LO + H::J_HI : 1;
+  static constexpr int NE  = WE0 * WE1 * WE2;
+  static constexpr int NJ  = WJ0 * WJ1 * WJ2;
+  // J window: FixedAcc<real>::WORDS planes of 3 * NJ 32-bit words
+  static constexpr int    WORDS      = FixedAcc<real>::WORDS;
+  static constexpr int    PLANE      = 3 * NJ;
+  static constexpr size_t eb_bytes   = sizeof(real) * 6 * (size_t)NE;
+  static constexpr size_t smem_bytes = ((eb_bytes + 15) / 16) * 16 + 4 * (size_t)WORDS * PLANE;
+};
+
+// wraps a ghost-free coordinate of a periodic axis into [0, n)
+__device__ __forceinline__ int wrap_periodic(int x, int n) {
+  x %= n;
+  return x < 0 ? x + n : x;
+}
+
+template <int D, int O, typename real>
+__global__ void __launch_bounds__(TileShape<D, real, O>::NT)
+    k_push_deposit_tiled(TiledArgs<real> a) {
+  using G               = TiledGeom<D, O, real>;
+  using H               = Halo<O>;
+  using FA              = FixedAcc<real>;
+  constexpr int  NT     = G::NT;
+  constexpr int  M      = kDriftMargin;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  real*          EBs = reinterpret_cast<real*>(smem_raw);
+  unsigned*      Jw  = reinterpret_cast<unsigned*>(smem_raw + ((G::eb_bytes + 15) / 16) * 16);
+  real*          Jr  = reinterpret_cast<real*>(Jw);  // real_t accumulation of dense tiles
+  __shared__ unsigned int s_qmax;  // bit pattern of the tile's largest |q w| max(1/dt, 1)
+
+  const int t  = blockIdx.x;
+  const int tx = t % a.ntiles[0];
+  const int ty = (t / a.ntiles[0]) % a.ntiles[1];
+  const int tz = D == 3 ? t / (a.ntiles[0] * a.ntiles[1]) : 0;
+  const int T0[3] = { tx * G::TX, ty * G::TY, tz * G::TZ };
+  const int ng    = a.pc.ng;
+
+  // 1. E/B window; reads ghost cells where the window overlaps them and the
+  //    periodic image beyond (zero beyond a non-periodic edge: no valid
+  //    particle's stencil reaches there)
+  for (int idx = threadIdx.x; idx < 6 * G::NE; idx += NT) {
+    int       r  = idx;
+    const int wi = r % G::WE0;
+    r /= G::WE0;
+    const int wj = r % G::WE1;
+    r /= G::WE1;
+    const int wk = r % G::WE2;
+    const int c  = r / G::WE2;
+    int       gc[3] = { T0[0] - H::E_LO + wi, T0[1] - H::E_LO + wj,
+                        D == 3 ? T0[2] - H::E_LO + wk : 0 };
+    bool      inside = true;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      if (gc[d] < -ng || gc[d] >= a.pc.n[d] + ng) {
+        if (a.periodic[d]) gc[d] = wrap_periodic(gc[d], a.pc.n[d]);
+        else inside = false;
+      }
+    }
+    EBs[idx] = inside ? a.EB.ld(gc[0] + ng, gc[1] + ng, D == 3 ? gc[2] + ng : 0, c) : (real)0;
+  }
+  for (int idx = threadIdx.x; idx < G::WORDS * G::PLANE; idx += NT) Jw[idx] = 0u;
+  // largest contribution bound of the tile, |q w| max(1/dt, 1), and its
+  // particle count (an upper bound on the additions any cell receives)
+  if (threadIdx.x == 0) s_qmax = 0u;
+  __syncthreads();
+  float   qmax = 0.f;
+  int64_t ntile = 0;
+  for (int s = 0; s < a.nsp; ++s) {
+    const real*   w  = (const real*)a.s[s].sp.w;
+    const float   qs = fabsf((float)a.s[s].charge);
+    const int64_t lo = a.s[s].tile_start[t], hi = a.s[s].tile_start[t + 1];
+    ntile += hi - lo;
+    for (int64_t p = lo + threadIdx.x; p < hi; p += NT) qmax = fmaxf(qmax, fabsf((float)w[p]) * qs);
+  }
+  qmax *= fmaxf((float)a.inv_dt, 1.f);
+  atomicMax(&s_qmax, __float_as_uint(qmax));  // non-negative floats order as their bits
+  __syncthreads();
+  const bool fixed = ntile <= FA::NMAX;
+  real       scale = 1, unscale = 1;
+  {
+    int ex = 0;
+    frexpf(__uint_as_float(s_qmax) * 1.0000002f, &ex);  // |contribution| < 2^ex
+    const int b = FA::bits(ntile);
+    scale   = (real)ldexp(1.0, b - ex);
+    unscale = (real)ldexp(1.0, ex - b);
+  }
+
+  const SmemView<real> ebv{ EBs, ng + T0[0] - H::E_LO, ng + T0[1] - H::E_LO,
+                            D == 3 ? ng + T0[2] - H::E_LO : 0, G::WE0, G::WE0 * G::WE1, G::NE };
+  const int joff[3] = { ng + T0[0] - H::J_LO, ng + T0[1] - H::J_LO,
+                        D == 3 ? ng + T0[2] - H::J_LO : 0 };
+
+  // 2. particles of the tile, species by species
+  for (int s = 0; s < a.nsp; ++s) {
+    const TiledSpecies<real>& S = a.s[s];
+    real*          ux[3]  = { (real*)S.sp.ux1, (real*)S.sp.ux2, (real*)S.sp.ux3 };
+    const real*    w      = (const real*)S.sp.w;
+    int32_t*       ia[3]  = { S.sp.i1, S.sp.i2, S.sp.i3 };
+    int32_t*       ipa[3] = { S.sp.i1p, S.sp.i2p, S.sp.i3p };
+    float*         da[3]  = { S.sp.dx1, S.sp.dx2, S.sp.dx3 };
+    float*         dpa[3] = { S.sp.dx1p, S.sp.dx2p, S.sp.dx3p };
+    const int64_t  lo = S.tile_start[t], hi = S.tile_start[t + 1];
+    for (int64_t p = lo + threadIdx.x; p < hi; p += NT) {
+      Prtl<real> q;
+      q.tag = S.sp.tag[p];
+      if (q.tag != PIC_TAG_ALIVE) {
+        if (q.tag != PIC_TAG_DEAD) atomicAdd(a.err + ERR_BAD_TAG, 1ull);
+        continue;
+      }
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        q.i[d]  = ia[d][p];
+        q.dx[d] = da[d][p];
+      }
+      if (!cells_in_grid<D>(q.i, a.pc.n)) {
+        atomicAdd(a.err + ERR_OUT_OF_GRID, 1ull);
+        continue;
+      }
+      bool near = true, edge = false;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const int T = d == 0 ? G::TX : (d == 1 ? G::TY : G::TZ);
+        near = near && (q.i[d] >= T0[d] - M) && (q.i[d] < T0[d] + T + M);
+        // a stencil that can reach the ghost layers of a non-periodic axis is
+        // deposited at the reference's coordinates: there the reference keeps
+        // the raw ghost currents, unfolded along the periodic axes
+        edge = edge || (!a.periodic[d] &&
+                        (q.i[d] < H::J_LO - M + 1 || q.i[d] >= a.pc.n[d] - (H::J_HI - M) - 1));
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) q.u[d] = ux[d][p];
+      real e0[3], b0[3];
+      int  ic[3] = { q.i[0] + ng, q.i[1] + ng, D == 3 ? q.i[2] + ng : 0 };
+      real dc[3] = { (real)q.dx[0], (real)q.dx[1], D == 3 ? (real)q.dx[2] : (real)0 };
+      if (near) {
+        if constexpr (O == 0) interp_zigzag<D, real>(ebv, ic, dc, e0, b0);
+        else                  interp_shape<D, O, real>(ebv, ic, dc, e0, b0);
+      } else {
+        // drifted past the margin: gather from global memory
+        if constexpr (O == 0) interp_zigzag<D, real>(a.EB, ic, dc, e0, b0);
+        else                  interp_shape<D, O, real>(a.EB, ic, dc, e0, b0);
+      }
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        e0[d] = e0[d] * a.dx;
+        b0[d] = b0[d] * a.dx;
+      }
+      if (S.vay) vay<real>(S.ndth, q.u, e0, b0);
+      else       boris<real>(S.ndth, q.u, e0, b0);
+      move_and_bound<D, real>(q, true, a.dt, a.dx, a.pc);
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        ia[d][p] = q.i[d];
+        da[d][p] = q.dx[d];
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) ux[d][p] = q.u[d];
+      if (q.tag != PIC_TAG_ALIVE) S.sp.tag[p] = q.tag;
+      if (a.write_prev) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          ipa[d][p] = q.ip[d];
+          dpa[d][p] = q.dxp[d];
+        }
+      }
+      if (q.tag == PIC_TAG_DEAD || S.charge == (real)0) continue;
+      if (edge || !near) {
+        // reference coordinates, global atomics
+        const FieldView<real>& J  = a.J;
+        const bool             ok = deposit_particle<D, O, real>(
+          q, w[p], S.charge, a.inv_dt, a.dx, ng, a.pc.ext,
+          [&](int i, int j, int k, int c, real v) { atomicAdd(J.p + J.idx(i, j, k, c), v); });
+        if (!ok) atomicAdd(a.err + ERR_STENCIL_OUT, 1ull);
+        continue;
+      }
+      // deposit at the coordinates before the periodic wrap (a shift of both
+      // i and i_prev by n leaves every contribution unchanged up to the image
+      // cell, which the flush folds back)
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        q.i[d] -= q.wrap[d];
+        q.ip[d] -= q.wrap[d];
+      }
+      const int jb = -joff[0] - joff[1] * G::WJ0 - joff[2] * (G::WJ0 * G::WJ1);
+      deposit_particle<D, O, real>(q, w[p], S.charge, a.inv_dt, a.dx, ng, nullptr,
+                                   [&](int i, int j, int k, int c, real v) {
+                                     const int e = jb + i + j * G::WJ0 +
+                                                   k * (G::WJ0 * G::WJ1) + c * G::NJ;
+                                     if (fixed) FA::add(Jw + e, G::PLANE, v, scale);
+                                     else       atomicAdd(Jr + e, v);
+                                   });
+    }
+  }
+  __syncthreads();
+
+  // 3. flush the J window (periodic images folded onto active cells)
+  for (int idx = threadIdx.x; idx < 3 * G::NJ; idx += NT) {
+    real v;
+    if (fixed) {
+      if (!FA::nonzero(Jw + idx, G::PLANE)) continue;
+      v = FA::value(Jw + idx, G::PLANE, unscale);
+    } else {
+      v = Jr[idx];
+      if (v == (real)0) continue;
+    }
+    int       r  = idx;
+    const int wi = r % G::WJ0;
+    r /= G::WJ0;
+    const int wj = r % G::WJ1;
+    r /= G::WJ1;
+    const int wk = r % G::WJ2;
+    const int c  = r / G::WJ2;
+    int       gc[3] = { T0[0] - H::J_LO + wi, T0[1] - H::J_LO + wj,
+                        D == 3 ? T0[2] - H::J_LO + wk : 0 };
+    bool      inside = true;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      if (a.periodic[d]) {
+        gc[d] = wrap_periodic(gc[d], a.pc.n[d]);
+      } else if (gc[d] < -ng || gc[d] >= a.pc.n[d] + ng) {
+        inside = false;
+      }
+    }
+    if (inside) {
+      atomicAdd(a.J.p + a.J.idx(gc[0] + ng, gc[1] + ng, D == 3 ? gc[2] + ng : 0, c), v);
+    } else {
+      atomicAdd(a.err + ERR_STENCIL_OUT, 1ull);
+    }
+  }
+}
+
+template <int D, int O, typename real>
+cudaError_t launch_push_deposit_tiled(const TiledArgs<real>& a, cudaStream_t s);
+
+// tile shape of a build, for the host (sort key and tile count)
+void tile_shape(int dim, int real_bytes, int order, int out[3]);
+
+}  // namespace pic

@@ -154,6 +154,11 @@ __global__ void k_keys(SortArgs a) {
       if (!ok) {
         atomicAdd(a.err + ERR_OUT_OF_GRID, 1ull);
         key = a.dead_bin;  // kept after the alive particles, tag untouched
+      } else if (a.tiled) {
+        const int tx = i1 / a.tile[0], ty = i2 / a.tile[1], tz = i3 / a.tile[2];
+        const int lx = i1 - tx * a.tile[0], ly = i2 - ty * a.tile[1], lz = i3 - tz * a.tile[2];
+        const int t  = (tz * a.ntiles[1] + ty) * a.ntiles[0] + tx;
+        key = (t * a.tile[2] + lz) * (a.tile[0] * a.tile[1]) + ly * a.tile[0] + lx;
       } else if (a.dim == 2) {
         key = i1 * a.n[1] + i2;
       } else {
@@ -307,6 +312,20 @@ template cudaError_t sort_apply<int32_t>(int32_t*, void*, const int32_t*, int64_
 template cudaError_t sort_apply<float>(float*, void*, const int32_t*, int64_t, cudaStream_t);
 template cudaError_t sort_apply<double>(double*, void*, const int32_t*, int64_t, cudaStream_t);
 template cudaError_t sort_apply<int16_t>(int16_t*, void*, const int32_t*, int64_t, cudaStream_t);
+
+namespace {
+__global__ void k_tile_offsets(const int64_t* off, int64_t tile_cells, int ntiles,
+                               int32_t* tile_start) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t <= ntiles) tile_start[t] = (int32_t)off[(int64_t)t * tile_cells];
+}
+}  // namespace
+
+cudaError_t tile_offsets(const int64_t* off, int64_t tile_cells, int ntiles, int32_t* tile_start,
+                         cudaStream_t s) {
+  PIC_KL(k_tile_offsets<<<(ntiles + 256) / 256, 256, 0, s>>>(off, tile_cells, ntiles, tile_start));
+  return cudaGetLastError();
+}
 
 cudaError_t set_tags(int16_t* tag, int64_t lo, int64_t hi, int16_t value, cudaStream_t s) {
   if (hi <= lo) return cudaSuccess;

@@ -41,6 +41,9 @@ struct SortArgs {
   int            dim;
   int            n[3];
   int            spatial;   // 1: cell key, 0: alive/dead only
+  int            tiled;     // with spatial: tile-major key (tile, then cell in tile)
+  int            tile[3];   // tile shape
+  int            ntiles[3]; // tiles per axis
   int32_t        dead_bin;  // index of the last bin
   // scratch
   int32_t*  key;
@@ -64,5 +67,9 @@ template <typename T>
 cudaError_t sort_apply(T* arr, void* tmp, const int32_t* perm, int64_t n, cudaStream_t s);
 
 cudaError_t set_tags(int16_t* tag, int64_t lo, int64_t hi, int16_t value, cudaStream_t s);
+
+// tile_start[t] = off[t * tile_cells] for t in [0, ntiles]
+cudaError_t tile_offsets(const int64_t* off, int64_t tile_cells, int ntiles, int32_t* tile_start,
+                         cudaStream_t s);
 
 }  // namespace pic

@@ -85,7 +85,10 @@ inline int SortParticles(Domain& dom, const pic_step_params& p, int64_t step, vo
   for (auto& s : dom.species) {
     uint32_t flags = 0;
     if (p.clear_interval > 0 && step % p.clear_interval == 0 && step > 0) flags |= PIC_SORT_REMOVE_DEAD;
-    if (p.sort_interval > 0 && step % p.sort_interval == 0) flags |= PIC_SORT_SPATIAL;
+    if (p.sort_interval > 0 && step % p.sort_interval == 0) {
+      flags |= PIC_SORT_SPATIAL;
+      if (p.sort_tiled) flags |= PIC_SORT_TILED;
+    }
     if (!flags) continue;
     if (!p.write_prev) flags |= PIC_SORT_SKIP_PREV;
     int64_t    n  = s.npart;

@@ -86,6 +86,11 @@ class Context:
         except Exception:
             pass
 
+    def tile_shape(self):
+        out = (C.c_int32 * 3)()
+        abi.call("pic_tile_shape", self.h, out)
+        return tuple(out)
+
     # --- field solvers -----------------------------------------------------
     def faraday(self, EB, coeff1, coeff2, stencil=None, stream=None):
         st = None if stencil is None else (C.c_double * 9)(*stencil)
@@ -167,7 +172,7 @@ class Context:
 
 def step_params(g: GridSpec, *, cfl, ppc0, skindepth0, larmor0, nfilter=0, sort_interval=0,
                 clear_interval=100, correction=1.0, write_prev=False, fieldsolver=True,
-                deposit=True):
+                deposit=True, sort_tiled=False):
     """Scales of SimulationParams (src/framework/parameters/parameters.cpp:47-78,
     algorithms.cpp:18-27, minkowski.h:82-84) in real_t arithmetic."""
     R = g.real
@@ -186,4 +191,5 @@ def step_params(g: GridSpec, *, cfl, ppc0, skindepth0, larmor0, nfilter=0, sort_
     p.nfilter, p.sort_interval, p.clear_interval = nfilter, sort_interval, clear_interval
     p.fieldsolver_enabled, p.deposit_enabled = int(fieldsolver), int(deposit)
     p.write_prev = int(write_prev)
+    p.sort_tiled = int(sort_tiled)
     return p

@@ -62,6 +62,14 @@ extern "C" {
 #define PIC_SORT_REMOVE_DEAD 1u /* Particles::RemoveDead before the spatial sort */
 #define PIC_SORT_SKIP_PREV 2u   /* leave i*_prev / dx*_prev arrays unpermuted */
 #define PIC_SORT_SPATIAL 4u     /* Particles::SortSpatially */
+/* With PIC_SORT_SPATIAL: order by tile of cells first, then by cell inside
+ * the tile (cells inside a tile i1-fastest), instead of the reference's
+ * i1-major cell key. The context then remembers each species' tile offsets
+ * and pic_push_deposit runs the tiled kernel for it until the species' npart
+ * changes or it is sorted again with another key. No reference counterpart:
+ * the reference's key only sets a traversal order, and this one lets a tile's
+ * particles be read as one contiguous range. */
+#define PIC_SORT_TILED 8u
 
 /* Grid and build choices of a domain (Grid/Mesh, src/framework/domain/grid.h;
  * N_GHOSTS and SHAPE_ORDER, src/global/global.h:130-136). Field element
@@ -120,6 +128,10 @@ int pic_destroy(pic_ctx* ctx);
 
 /* Copy of the grid the context was created with. */
 int pic_get_grid(const pic_ctx* ctx, pic_grid* out);
+
+/* Cells per tile along each axis used by PIC_SORT_TILED and the tiled
+ * push/deposit of this context (no reference counterpart). */
+int pic_tile_shape(const pic_ctx* ctx, int32_t out[3]);
 
 /* srpic::Faraday (src/engines/srpic/fieldsolvers.h:36-99) with
  * Faraday_kernel (src/kernels/faraday_mink.hpp:71-166), fused with
@@ -243,6 +255,7 @@ typedef struct {
   int32_t fieldsolver_enabled;
   int32_t deposit_enabled;
   int32_t write_prev;
+  int32_t sort_tiled; /* spatial sorts use PIC_SORT_TILED */
 } pic_step_params;
 
 int pic_srpic_step(pic_ctx* ctx, pic_species* sp, int32_t nspecies, void* EB, void* J,

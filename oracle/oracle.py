@@ -54,6 +54,7 @@ def lib(real):
         L.orc_fill_ghosts.argtypes = [G, V, C.c_int, C.c_int, C.c_int]
         L.orc_sync_currents.argtypes = [G, V, V]
         L.orc_sort.argtypes = [G, S, C.POINTER(C.c_int64)]
+        L.orc_sort_tiled.argtypes = [G, S, C.POINTER(C.c_int), C.POINTER(C.c_int64)]
         L.orc_remove_dead.restype = C.c_int64
         L.orc_remove_dead.argtypes = [G, S]
         L.orc_field_energy.argtypes = [G, V, C.c_double, C.POINTER(C.c_double)]
@@ -135,6 +136,14 @@ class Oracle:
         s = self.species(sp)
         perm = torch.empty(max(sp.npart, 1), dtype=torch.int64)
         self.L.orc_sort(C.byref(self.og), C.byref(s), C.cast(perm.data_ptr(), C.POINTER(C.c_int64)))
+        return perm[:sp.npart]
+
+    def sort_tiled(self, sp, tile):
+        s = self.species(sp)
+        perm = torch.empty(max(sp.npart, 1), dtype=torch.int64)
+        ts = (C.c_int * 3)(*tile)
+        self.L.orc_sort_tiled(C.byref(self.og), C.byref(s), ts,
+                              C.cast(perm.data_ptr(), C.POINTER(C.c_int64)))
         return perm[:sp.npart]
 
     def remove_dead(self, sp):

@@ -1060,14 +1060,30 @@ static void permute_all(const orc_grid* g, orc_species* sp, const int64_t* perm)
   PERMUTE(int16_t, sp->tag);
 }
 
-void orc_sort(const orc_grid* g, orc_species* sp, int64_t* perm) {
+/* tile: NULL for the reference's cell key, else the tile shape of the
+ * tile-major key (tile index i1-fastest over tiles, then the cell inside the
+ * tile i1-fastest) that the GPU's tiled sort uses */
+static void sort_keyed(const orc_grid* g, orc_species* sp, const int* tile, int64_t* perm) {
   const int64_t np    = sp->npart;
-  const int64_t total = (int64_t)g->n1 * g->n2 * (g->dim == 3 ? g->n3 : 1);
+  int           nt[3] = { 1, 1, 1 }, ts[3] = { 1, 1, 1 };
+  const int     nn[3] = { g->n1, g->n2, g->dim == 3 ? g->n3 : 1 };
+  if (tile) {
+    for (int d = 0; d < 3; ++d) {
+      ts[d] = d < g->dim ? tile[d] : 1;
+      nt[d] = (nn[d] + ts[d] - 1) / ts[d];
+    }
+  }
+  const int64_t total = tile ? (int64_t)nt[0] * nt[1] * nt[2] * ts[0] * ts[1] * ts[2]
+                             : (int64_t)g->n1 * g->n2 * (g->dim == 3 ? g->n3 : 1);
   int64_t*      key   = (int64_t*)malloc(sizeof(int64_t) * (size_t)(np > 0 ? np : 1));
   int64_t*      cnt   = (int64_t*)calloc((size_t)(total + 3), sizeof(int64_t));
   for (int64_t p = 0; p < np; ++p) {
     if (sp->tag[p] != ORC_TAG_ALIVE) {
       key[p] = total + 1; /* sorting.h:114-116 */
+    } else if (tile) {
+      const int     c[3] = { sp->i1[p], sp->i2[p], g->dim == 3 ? sp->i3[p] : 0 };
+      const int64_t t    = ((int64_t)(c[2] / ts[2]) * nt[1] + c[1] / ts[1]) * nt[0] + c[0] / ts[0];
+      key[p] = ((t * ts[2] + c[2] % ts[2]) * ts[1] + c[1] % ts[1]) * ts[0] + c[0] % ts[0];
     } else if (g->dim == 2) {
       key[p] = (int64_t)sp->i1[p] * g->n2 + sp->i2[p];
     } else {
@@ -1082,10 +1098,17 @@ void orc_sort(const orc_grid* g, orc_species* sp, int64_t* perm) {
   free(cnt);
 }
 
+void orc_sort(const orc_grid* g, orc_species* sp, int64_t* perm) { sort_keyed(g, sp, NULL, perm); }
+
+void orc_sort_tiled(const orc_grid* g, orc_species* sp, const int* tile, int64_t* perm) {
+  sort_keyed(g, sp, tile, perm);
+}
+
 int64_t orc_remove_dead(const orc_grid* g, orc_species* sp) {
   const int64_t np = sp->npart;
   int64_t*      perm = (int64_t*)malloc(sizeof(int64_t) * (size_t)(np > 0 ? np : 1));
   int64_t       na   = 0;
+  if (!perm) return np;
   for (int64_t p = 0; p < np; ++p)
     if (sp->tag[p] == ORC_TAG_ALIVE) perm[na++] = p;
   int64_t nd = na;

@@ -112,6 +112,12 @@ void orc_sync_currents(const orc_grid* g, void* J, void* buff);
  * every array of the species in place. */
 void orc_sort(const orc_grid* g, orc_species* sp, int64_t* perm);
 
+/* The same stable counting sort on the GPU path's tile-major key (tile
+ * index i1-fastest over tiles of shape tile[0..2], then the cell inside the
+ * tile i1-fastest); checks PIC_SORT_TILED, which has no reference
+ * counterpart. */
+void orc_sort_tiled(const orc_grid* g, orc_species* sp, const int* tile, int64_t* perm);
+
 /* Particles::RemoveDead (src/framework/containers/particles_sort.cpp:103-194):
  * stable compaction of alive particles, tags reset, returns new npart. */
 int64_t orc_remove_dead(const orc_grid* g, orc_species* sp);

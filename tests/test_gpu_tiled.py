@@ -1,0 +1,162 @@
+"""The tiled push/deposit path (PIC_SORT_TILED + shared-memory windows).
+
+After a tiled sort the particle order differs from the reference's cell key,
+so the oracle starts from the GPU-sorted arrays; the bars are those of the
+untiled path: particles bit-exact, J to round-off (summation order only).
+Multi-step runs without re-sorting let particles drift past the window's
+margin, which exercises the global-memory fallback inside the same kernel.
+"""
+import pytest
+import torch
+
+from entity_gb300 import abi
+from entity_gb300.inputs import GridSpec, empty_field, make_species
+from entity_gb300.sim import Context
+from tests.helpers import random_fields
+from tests.test_gpu_parity import J_TOL, _assert_J_close, _assert_particles_equal
+
+pytestmark = pytest.mark.gpu
+
+REALS = [torch.float32, torch.float64]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from entity_gb300 import build
+    build.build()
+    abi.load()
+
+
+def _oracle(g):
+    from oracle.oracle import Oracle
+    return Oracle(g)
+
+
+def _grid(dim, order, real, **kw):
+    # sizes that leave partial tiles at the upper edges
+    n = (72, 40, 1) if dim == 2 else (20, 12, 10)
+    return GridSpec(dim=dim, n=n, order=order, real=real, **kw)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("real", REALS)
+def test_tiled_sort_matches_oracle(dim, real):
+    g = _grid(dim, 2, real)
+    sp = make_species(g, 5, 0.2, 0.0, 7)
+    sp.tag[::17] = 0
+    spg = sp.clone().to("cuda")
+    ctx = Context(g)
+    tile = ctx.tile_shape()
+    _oracle(g).sort_tiled(sp, tile)
+    assert ctx.sort(spg, abi.PIC_SORT_SPATIAL | abi.PIC_SORT_TILED) == abi.PIC_OK
+    _assert_particles_equal(sp, spg, dim)
+
+
+def _tiled_pair(g, seeds, temp, beta=0.3, **kw):
+    """GPU species sorted by tile, and CPU copies in the same order."""
+    ctx = Context(g)
+    gpu, cpu = [], []
+    for k, sd in enumerate(seeds):
+        s = make_species(g, 4, temp, beta if k == 0 else -beta, sd,
+                         charge=-1.0 if k == 0 else 1.0, index=k + 1, **kw).to("cuda")
+        assert ctx.sort(s, abi.PIC_SORT_SPATIAL | abi.PIC_SORT_TILED) == abi.PIC_OK
+        gpu.append(s)
+        cpu.append(s.clone().to("cpu"))
+    return ctx, gpu, cpu
+
+
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("order", [0, 1, 2, 3])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_tiled_push_deposit(dim, order, real):
+    g = _grid(dim, order, real)
+    EB = random_fields(g, 5 + order)
+    ctx, gpu, cpu = _tiled_pair(g, [31, 32], temp=0.3)
+    o = _oracle(g)
+    Jo = empty_field(g, 3)
+    for s in cpu:
+        o.push(s, EB, 0.45, 0.7, g.dx)
+    o.deposit(cpu, Jo, 0.45, g.dx)
+    o.sync_currents(Jo, empty_field(g, 3))
+    o.fill_ghosts(Jo, False, 0, 3)
+    Jg = empty_field(g, 3, "cuda")
+    ctx.push_deposit(gpu, EB.cuda(), Jg, 0.45, 0.7, g.dx, flags=abi.PIC_PD_WRITE_PREV)
+    ctx.sync_currents(Jg)
+    torch.cuda.synchronize()
+    for a, b in zip(cpu, gpu):
+        _assert_particles_equal(a, b, dim)
+    _assert_J_close(Jo, Jg, real)
+    assert ctx.device_errors() == [0, 0, 0, 0]
+
+
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("dim,order", [(2, 1), (3, 2), (3, 3)])
+def test_tiled_drift_beyond_margin(dim, order, real):
+    # relativistic plasma pushed 8 times without re-sorting: the farthest
+    # particles leave their tile by more than the drift margin
+    g = _grid(dim, order, real)
+    EB = random_fields(g, 77, amp=0.1)
+    ctx, gpu, cpu = _tiled_pair(g, [41, 42], temp=2.0, beta=0.5)
+    o = _oracle(g)
+    EBg = EB.cuda()
+    for step in range(8):
+        Jo = empty_field(g, 3)
+        for s in cpu:
+            o.push(s, EB, 0.45, 0.7, g.dx)
+        o.deposit(cpu, Jo, 0.45, g.dx)
+        o.sync_currents(Jo, empty_field(g, 3))
+        Jg = empty_field(g, 3, "cuda")
+        ctx.push_deposit(gpu, EBg, Jg, 0.45, 0.7, g.dx, flags=abi.PIC_PD_WRITE_PREV)
+        ctx.sync_currents(Jg)
+        torch.cuda.synchronize()
+        for a, b in zip(cpu, gpu):
+            _assert_particles_equal(a, b, dim)
+        # compare the active cells (the oracle leaves raw deposits in ghosts)
+        ng = g.ng
+        sl = (slice(None), slice(None), slice(ng, -ng), slice(ng, -ng)) if dim == 2 else \
+            (slice(None), slice(ng, -ng), slice(ng, -ng), slice(ng, -ng))
+        _assert_J_close(Jo[sl], Jg[sl], real)
+
+
+@pytest.mark.parametrize("bc", [abi.PIC_BC_ABSORB, abi.PIC_BC_REFLECT])
+def test_tiled_non_periodic_boundaries(bc):
+    g = GridSpec(dim=3, n=(20, 12, 10), order=2, real=torch.float32, periodic=(0, 1, 1),
+                 prtl_bc=((bc, bc), (0, 0), (0, 0)))
+    EB = random_fields(g, 9)
+    ctx, gpu, cpu = _tiled_pair(g, [51, 52], temp=1.0)
+    o = _oracle(g)
+    Jo = empty_field(g, 3)
+    for s in cpu:
+        o.push(s, EB, 0.45, 0.7, g.dx)
+    o.deposit(cpu, Jo, 0.45, g.dx)
+    o.sync_currents(Jo, empty_field(g, 3))
+    o.fill_ghosts(Jo, False, 0, 3)
+    Jg = empty_field(g, 3, "cuda")
+    ctx.push_deposit(gpu, EB.cuda(), Jg, 0.45, 0.7, g.dx, flags=abi.PIC_PD_WRITE_PREV)
+    ctx.sync_currents(Jg)
+    torch.cuda.synchronize()
+    for a, b in zip(cpu, gpu):
+        _assert_particles_equal(a, b, 3)
+    # periodic axes folded; along the open axis the ghosts keep raw deposits
+    _assert_J_close(Jo, Jg, torch.float32)
+
+
+def test_tiled_falls_back_when_npart_changes():
+    g = _grid(3, 2, torch.float32)
+    EB = random_fields(g, 3)
+    ctx, gpu, cpu = _tiled_pair(g, [61], temp=0.3)
+    s = gpu[0]
+    s.npart -= 10     # the binning no longer describes the arrays
+    c = cpu[0]
+    c.npart -= 10
+    o = _oracle(g)
+    Jo = empty_field(g, 3)
+    o.push(c, EB, 0.45, 0.7, g.dx)
+    o.deposit([c], Jo, 0.45, g.dx)
+    Jg = empty_field(g, 3, "cuda")
+    ctx.push_deposit([s], EB.cuda(), Jg, 0.45, 0.7, g.dx, flags=abi.PIC_PD_WRITE_PREV)
+    torch.cuda.synchronize()
+    _assert_particles_equal(c, s, 3)
+    _assert_J_close(Jo, Jg, torch.float32)
