@@ -108,6 +108,8 @@ SIGNATURES = {
     "pic_fill_ghosts": (C.c_int, [_VP, _VP, C.c_int32, C.c_int32, C.c_int32, _VP]),
     "pic_sort": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_uint32, C.POINTER(C.c_int64), _VP]),
     "pic_field_energy": (C.c_int, [_VP, _VP, C.c_double, C.POINTER(C.c_double), _VP]),
+    "pic_field_energy_noalloc": (C.c_int, [C.POINTER(PicGrid), _VP, C.c_double,
+                                           C.POINTER(C.c_double), _VP]),
     "pic_get_device_errors": (C.c_int, [_VP, C.POINTER(C.c_int64), C.c_int32, _VP]),
     "pic_srpic_step": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32, _VP, _VP, _VP,
                                  C.POINTER(PicStepParams), C.c_int64, _VP]),

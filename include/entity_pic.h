@@ -209,6 +209,21 @@ int pic_sort(pic_ctx* ctx, pic_species* sp, uint32_t flags, int64_t* npart_out, 
  * Synchronises the stream. */
 int pic_field_energy(pic_ctx* ctx, const void* EB, double dx, double* out, void* stream);
 
+/* The field energy of pic_field_energy for callers that cannot allocate
+ * device memory (a framework that reserves all device memory for its own
+ * pool, a between-steps hook where cudaMalloc could synchronise the device,
+ * a fixed device-memory budget). No counterpart in the reference. Needs no
+ * context: it takes the grid description directly and allocates nothing; its
+ * scratch is a fixed 1 MiB array inside the library, one slot pair per grid
+ * row, so grids with more than 65536 rows (n2 * n3 in 3D, n2 in 2D) are
+ * rejected with PIC_ERR_UNSUPPORTED. The first call on a device resolves the
+ * array's device address, so make it before any stream capture. Calls share
+ * the array: calls that overlap on the GPU race and must be serialised. The
+ * result is computed in a fixed order (bitwise reproducible). Synchronises
+ * the stream. */
+int pic_field_energy_noalloc(const pic_grid* grid, const void* EB, double dx, double* out,
+                             void* stream);
+
 /* Device error word: out[0] = particles with an invalid tag seen by the
  * pusher, out[1] = alive particles whose cell lies outside the grid (skipped
  * by the pusher, reported by the sort), out[2] = particles whose deposit
