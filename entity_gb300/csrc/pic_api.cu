@@ -50,6 +50,10 @@ struct SpeciesBins {
   int32_t* tile_start = nullptr;
   int      ntiles     = 0;
   bool     valid      = false;
+  // particles the tiled kernel leaves to the per-particle kernel
+  int32_t*  ovf       = nullptr;  // capacity ovf_cap
+  unsigned* ovf_count = nullptr;
+  int64_t   ovf_cap   = 0;
 };
 
 struct pic_ctx {
@@ -272,6 +276,10 @@ int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void
     a.s[k].ndth           = (real)0.5 * (real)qm * (real)omegaB0 * (real)dt;
     a.s[k].charge         = (real)sp->charge;
     a.s[k].vay            = sp->pusher == PIC_PUSHER_VAY;
+    SpeciesBins* b        = find_bins(c, sp->index, false);
+    a.s[k].ovf            = b->ovf;
+    a.s[k].ovf_count      = b->ovf_count;
+    if (cudaMemsetAsync(b->ovf_count, 0, sizeof(unsigned), s) != cudaSuccess) return PIC_ERR_CUDA;
   }
   int ts[3];
   ntiles_of(c, a.ntiles, ts);
@@ -303,7 +311,29 @@ int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void
   PIC_TD(3, 2)
   PIC_TD(3, 3)
 #undef PIC_TD
-  return cuda_status(e);
+  if (e != cudaSuccess) return PIC_ERR_CUDA;
+  // the particles the tiled kernel deferred: per-particle kernel over the list
+  for (int k = 0; k < a.nsp; ++k) {
+    const pic_species* sp = sps[k];
+    pic::PDArgs<real>  pa;
+    pa.sp = sptrs(sp);
+    pa.pc = a.pc;
+    pa.EB = a.EB;
+    pa.J  = a.J;
+    pa.dt = a.dt;
+    pa.dx = a.dx;
+    pa.ndth       = a.s[k].ndth;
+    pa.inv_dt     = a.inv_dt;
+    pa.charge     = a.s[k].charge;
+    pa.vay        = a.s[k].vay;
+    pa.write_prev = a.write_prev;
+    pa.err        = a.err;
+    pa.list       = a.s[k].ovf;
+    pa.list_count = a.s[k].ovf_count;
+    e = pd_dispatch<real>(c, pa, pic::MODE_FUSED, false, s);
+    if (e != cudaSuccess) return PIC_ERR_CUDA;
+  }
+  return PIC_OK;
 }
 
 template <typename real>
@@ -384,7 +414,11 @@ int pic_destroy(pic_ctx* c) {
   cudaDeviceSynchronize();
   pic_timers_reset(c);
   for (auto e : c->event_pool) cudaEventDestroy(e);
-  for (auto& b : c->bins) cudaFree(b.tile_start);
+  for (auto& b : c->bins) {
+    cudaFree(b.tile_start);
+    cudaFree(b.ovf);
+    cudaFree(b.ovf_count);
+  }
   cudaFree(c->d_err);
   cudaFree(c->d_energy);
   if (c->sort_buf) cudaFree(c->sort_buf);
@@ -794,6 +828,17 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
     }
     if ((e = pic::tile_offsets(a.off, tcells, (int)ntiles, b->tile_start, s)) != cudaSuccess)
       return PIC_ERR_CUDA;
+    const int64_t cap = np - n_dead;  // every binned particle may end up deferred
+    if (b->ovf_cap < cap || !b->ovf_count) {
+      cudaFree(b->ovf);
+      b->ovf = nullptr;
+      b->ovf_cap = 0;
+      if (!b->ovf_count && cudaMalloc((void**)&b->ovf_count, sizeof(unsigned)) != cudaSuccess)
+        return PIC_ERR_NOMEM;
+      if (cudaMalloc((void**)&b->ovf, sizeof(int32_t) * (cap > 0 ? cap : 1)) != cudaSuccess)
+        return PIC_ERR_NOMEM;
+      b->ovf_cap = cap;
+    }
     b->nalive = np - n_dead;
     b->npart  = newn;
     b->valid  = true;

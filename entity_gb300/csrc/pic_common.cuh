@@ -528,99 +528,110 @@ __device__ __forceinline__ bool deposit_particle(const Prtl<real>& q, real weigh
     const real Q     = coeff * inv_dt;
     const int  d1 = imax[0] - imin[0], d2 = imax[1] - imin[1];
     const int  i0 = imin[0] + ng, j0 = imin[1] + ng;
+    // Every entry of the (O+2)-wide stencil is computed and only the add is
+    // predicated on the stencil extent: the loops carry no divergent
+    // branches. Each entry's arithmetic is the reference's expression; the
+    // factors that do not depend on the innermost index are formed once.
     if constexpr (D == 2) {
       const real QVx3 = coeff * vp[2];
-      // jx1: prefix over i
+      real hd0[N], hs0[N];  // HALF * (fS - iS), HALF * (fS + iS) along x1
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        hd0[i] = HALF * (fS[0][i] - iS[0][i]);
+        hs0[i] = HALF * (fS[0][i] + iS[0][i]);
+      }
+      // jx1: prefix over i (currents_deposit.hpp:496-518, 547-551)
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        if (j > d2) break;
-        real acc = 0;
+        const real s1 = fS[1][j] + iS[1][j];
+        real       acc = 0;
 #pragma unroll
         for (int i = 0; i < N - 1; ++i) {
-          if (i >= d1) break;
-          const real W = HALF * (fS[0][i] - iS[0][i]) * (fS[1][j] + iS[1][j]);
+          const real W = hd0[i] * s1;
           acc          = (i == 0) ? (-Q * W) : (acc - Q * W);
-          add(i0 + i, j0 + j, 0, 0, acc);
+          if (i < d1 && j <= d2) add(i0 + i, j0 + j, 0, 0, acc);
         }
       }
       // jx2: prefix over j
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        if (i > d1) break;
         real acc = 0;
 #pragma unroll
         for (int j = 0; j < N - 1; ++j) {
-          if (j >= d2) break;
-          const real W = HALF * (fS[0][i] + iS[0][i]) * (fS[1][j] - iS[1][j]);
+          const real W = hs0[i] * (fS[1][j] - iS[1][j]);
           acc          = (j == 0) ? (-Q * W) : (acc - Q * W);
-          add(i0 + i, j0 + j, 0, 1, acc);
+          if (i <= d1 && j < d2) add(i0 + i, j0 + j, 0, 1, acc);
         }
       }
+      // jx3
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        if (i > d1) break;
+        const real ga = HALF * iS[0][i] + fS[0][i];
+        const real gb = HALF * fS[0][i] + iS[0][i];
 #pragma unroll
         for (int j = 0; j < N; ++j) {
-          if (j > d2) break;
-          const real W = THIRD * (fS[1][j] * (HALF * iS[0][i] + fS[0][i]) +
-                                  iS[1][j] * (HALF * fS[0][i] + iS[0][i]));
-          add(i0 + i, j0 + j, 0, 2, QVx3 * W);
+          const real W = THIRD * (fS[1][j] * ga + iS[1][j] * gb);
+          if (i <= d1 && j <= d2) add(i0 + i, j0 + j, 0, 2, QVx3 * W);
         }
       }
     } else {
       const int d3 = imax[2] - imin[2];
       const int k0 = imin[2] + ng;
+      real      t0[N], t1[N], t2[N];  // THIRD * (fS - iS) per axis
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        t0[i] = THIRD * (fS[0][i] - iS[0][i]);
+        t1[i] = THIRD * (fS[1][i] - iS[1][i]);
+        t2[i] = THIRD * (fS[2][i] - iS[2][i]);
+      }
+      // jx1: prefix over i (currents_deposit.hpp:620-700, 716-724)
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        if (j > d2) break;
 #pragma unroll
         for (int k = 0; k < N; ++k) {
-          if (k > d3) break;
-          real acc = 0;
+          const real P = (iS[1][j] * iS[2][k] + fS[1][j] * fS[2][k]) +
+                         HALF * (iS[2][k] * fS[1][j] + iS[1][j] * fS[2][k]);
+          const bool ok = (j <= d2) && (k <= d3);
+          real       acc = 0;
 #pragma unroll
           for (int i = 0; i < N - 1; ++i) {
-            if (i >= d1) break;
-            const real W = THIRD * (fS[0][i] - iS[0][i]) *
-                           ((iS[1][j] * iS[2][k] + fS[1][j] * fS[2][k]) +
-                            HALF * (iS[2][k] * fS[1][j] + iS[1][j] * fS[2][k]));
-            acc = (i == 0) ? (-Q * W) : (acc - Q * W);
-            add(i0 + i, j0 + j, k0 + k, 0, acc);
+            const real W = t0[i] * P;
+            acc          = (i == 0) ? (-Q * W) : (acc - Q * W);
+            if (ok && i < d1) add(i0 + i, j0 + j, k0 + k, 0, acc);
           }
         }
       }
+      // jx2: prefix over j
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        if (i > d1) break;
 #pragma unroll
         for (int k = 0; k < N; ++k) {
-          if (k > d3) break;
-          real acc = 0;
+          const real P = iS[0][i] * iS[2][k] + fS[0][i] * fS[2][k] +
+                         HALF * (iS[2][k] * fS[0][i] + iS[0][i] * fS[2][k]);
+          const bool ok = (i <= d1) && (k <= d3);
+          real       acc = 0;
 #pragma unroll
           for (int j = 0; j < N - 1; ++j) {
-            if (j >= d2) break;
-            const real W = THIRD * (fS[1][j] - iS[1][j]) *
-                           (iS[0][i] * iS[2][k] + fS[0][i] * fS[2][k] +
-                            HALF * (iS[2][k] * fS[0][i] + iS[0][i] * fS[2][k]));
-            acc = (j == 0) ? (-Q * W) : (acc - Q * W);
-            add(i0 + i, j0 + j, k0 + k, 1, acc);
+            const real W = t1[j] * P;
+            acc          = (j == 0) ? (-Q * W) : (acc - Q * W);
+            if (ok && j < d2) add(i0 + i, j0 + j, k0 + k, 1, acc);
           }
         }
       }
+      // jx3: prefix over k
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        if (i > d1) break;
 #pragma unroll
         for (int j = 0; j < N; ++j) {
-          if (j > d2) break;
-          real acc = 0;
+          const real P = iS[0][i] * iS[1][j] + fS[0][i] * fS[1][j] +
+                         HALF * (iS[0][i] * fS[1][j] + iS[1][j] * fS[0][i]);
+          const bool ok = (i <= d1) && (j <= d2);
+          real       acc = 0;
 #pragma unroll
           for (int k = 0; k < N - 1; ++k) {
-            if (k >= d3) break;
-            const real W = THIRD * (fS[2][k] - iS[2][k]) *
-                           (iS[0][i] * iS[1][j] + fS[0][i] * fS[1][j] +
-                            HALF * (iS[0][i] * fS[1][j] + iS[1][j] * fS[0][i]));
-            acc = (k == 0) ? (-Q * W) : (acc - Q * W);
-            add(i0 + i, j0 + j, k0 + k, 2, acc);
+            const real W = t2[k] * P;
+            acc          = (k == 0) ? (-Q * W) : (acc - Q * W);
+            if (ok && k < d3) add(i0 + i, j0 + j, k0 + k, 2, acc);
           }
         }
       }

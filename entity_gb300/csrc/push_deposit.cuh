@@ -24,6 +24,10 @@ struct PDArgs {
   int             vay;
   int             write_prev;
   unsigned long long* err;
+  // optional: process only the particles listed (indices into the arrays),
+  // *list_count of them (a device counter)
+  const int32_t*  list       = nullptr;
+  const unsigned* list_count = nullptr;
 };
 
 template <int D, int O, typename real, int MODE, bool PHOTON>
@@ -35,8 +39,10 @@ __global__ void __launch_bounds__(256) k_push_deposit(PDArgs<real> a) {
   int32_t*      ipa[3] = { a.sp.i1p, a.sp.i2p, a.sp.i3p };
   float*        da[3]  = { a.sp.dx1, a.sp.dx2, a.sp.dx3 };
   float*        dpa[3] = { a.sp.dx1p, a.sp.dx2p, a.sp.dx3p };
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.sp.npart; p += stride) {
-    Prtl<real> q;
+  const int64_t n = a.list ? (int64_t)*a.list_count : a.sp.npart;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += stride) {
+    const int64_t p = a.list ? (int64_t)a.list[t] : t;
+    Prtl<real>    q;
     q.tag = a.sp.tag[p];
     if constexpr (MODE == MODE_DEPOSIT) {
       if (q.tag == PIC_TAG_DEAD) continue;

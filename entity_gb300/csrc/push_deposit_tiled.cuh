@@ -17,9 +17,9 @@
 // combine lanes that hit the same address; float, double and 64-bit integer
 // shared atomics serialise such lanes, and cell-sorted particles make these
 // collisions the common case. Each tile scales contributions by a power of
-// two 2^s so that |v 2^s| < 2^b, converts to a 64-bit integer (exact up to
-// the quantisation 2^-s) and adds it as 32-bit words: a 12-bit low word and a
-// signed high word (float), or three 16-bit words and a signed top word
+// two 2^s so that |v 2^s| < 2^b, rounds them to integers (exact up to the
+// quantisation 2^-s) and adds them as 32-bit words: X = 4096 hi + lo with
+// lo in [-2048, 2048] (float), or three 16-bit words and a signed top word
 // (double). With N particles in the tile no cell takes more than N additions
 // per component, so b = 43 - log2 N (float; 29 bits at 16k particles) or
 // b = 62 - log2 N (double) overflows neither a word nor the 64-bit total.
@@ -29,9 +29,13 @@
 // 2^16 in double) accumulates in real_t atomics instead.
 //
 // A particle that has drifted more than M cells outside its tile since the
-// last tiled sort gathers E/B from global memory and deposits with global
-// atomics instead, so results never depend on the sort interval.
-// Arithmetic per particle is the same code as the untiled kernel.
+// last tiled sort, or whose stencil can reach the ghost layers of a
+// non-periodic axis, is not touched here: it is appended to the species'
+// overflow list and pushed afterwards by the per-particle kernel (global
+// gathers, global atomics, the reference's coordinates). Results therefore
+// never depend on the sort interval, and the hot kernel holds only the
+// shared-memory path. Arithmetic per particle is the same code as the
+// untiled kernel.
 #pragma once
 
 #include <type_traits>
@@ -49,17 +53,30 @@ struct FixedAcc;
 template <>
 struct FixedAcc<float> {
   static constexpr int     WORDS = 2;
-  static constexpr int64_t NMAX  = 1 << 20;  // low-word sums stay below 2^32
-  __device__ static int bits(int64_t n) { return 43 - (n > 1 ? 64 - __clzll(n - 1) : 0); }
-  __device__ static void add(unsigned* w, int plane, float v, float scale) {
-    const long long X = __float2ll_rn(v * scale);
-    atomicAdd(w, (unsigned)(X & 0xFFF));
-    atomicAdd(w + plane, (unsigned)(int)(X >> 12));
+  static constexpr int64_t NMAX  = (1 << 20) - 1;  // |low-word sums| stay below 2^31
+  // b = 43 - log2 N, capped at 34 so that v / 4096 stays inside the
+  // rounding trick's 2^22 range
+  __device__ static int bits(int64_t n) { return min(34, 43 - (n > 1 ? 64 - __clzll(n - 1) : 0)); }
+  // v arrives already scaled by 2^s (|v| < 2^b). X = round(v) is split as
+  // X = hi * 4096 + lo, lo in [-2048, 2048], with float arithmetic only:
+  // adding 1.5 * 2^23 rounds a float of magnitude < 2^22 to an integer held
+  // in the low mantissa bits (conversions to 64-bit integers would run on
+  // the GPU's narrow FP64 pipe). Every step is exact except the two
+  // intended roundings to integers.
+  __device__ static void add(unsigned* w, int plane, float v) {
+    constexpr float    MAGIC = 12582912.0f;  // 1.5 * 2^23
+    constexpr unsigned MBITS = 0x4B400000u;
+    const float t  = __fmaf_rn(v, 1.0f / 4096.0f, MAGIC);  // MAGIC + round(v / 4096)
+    const float hf = __fsub_rn(t, MAGIC);                   // round(v / 4096), exact
+    const float lf = __fmaf_rn(hf, -4096.0f, v);            // v - 4096 hi, exact
+    const float lt = __fadd_rn(lf, MAGIC);                  // MAGIC + round(lf)
+    atomicAdd(w, __float_as_uint(lt) - MBITS);
+    atomicAdd(w + plane, __float_as_uint(t) - MBITS);
   }
   __device__ static bool nonzero(const unsigned* w, int plane) { return (w[0] | w[plane]) != 0u; }
   __device__ static float value(const unsigned* w, int plane, float unscale) {
-    const unsigned long long t = ((unsigned long long)(long long)(int)w[plane] << 12) + w[0];
-    return __ll2float_rn((long long)t) * unscale;
+    const long long t = (long long)(int)w[plane] * 4096 + (long long)(int)w[0];
+    return __ll2float_rn(t) * unscale;
   }
 };
 template <>
@@ -68,8 +85,8 @@ struct FixedAcc<double> {
   static constexpr int64_t NMAX  = 1 << 16;  // 16-bit word sums stay below 2^32
   // the 64-bit total of N additions must not overflow either
   __device__ static int bits(int64_t n) { return 62 - (n > 1 ? 64 - __clzll(n - 1) : 0); }
-  __device__ static void add(unsigned* w, int plane, double v, double scale) {
-    const long long X = __double2ll_rn(v * scale);
+  __device__ static void add(unsigned* w, int plane, double v) {
+    const long long X = __double2ll_rn(v);  // v arrives scaled by 2^s
     atomicAdd(w, (unsigned)(X & 0xFFFF));
     atomicAdd(w + plane, (unsigned)((X >> 16) & 0xFFFF));
     atomicAdd(w + 2 * plane, (unsigned)((X >> 32) & 0xFFFF));
@@ -117,6 +134,8 @@ struct TiledSpecies {
   const int32_t* tile_start;  // ntiles + 1 offsets into the particle arrays
   real           ndth, charge;
   int            vay;
+  int32_t*       ovf;         // particles left to the per-particle kernel
+  unsigned*      ovf_count;
 };
 
 template <typename real>
@@ -273,19 +292,29 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
         edge = edge || (!a.periodic[d] &&
                         (q.i[d] < H::J_LO - M + 1 || q.i[d] >= a.pc.n[d] - (H::J_HI - M) - 1));
       }
+      {
+        // particles that drifted past the margin, or whose stencil can reach
+        // the ghost layers of a non-periodic axis, are left to the
+        // per-particle kernel (global gathers, reference coordinates)
+        const bool     defer = !near || edge;
+        const unsigned ball  = __ballot_sync(__activemask(), defer);
+        if (defer) {
+          const int      lane   = threadIdx.x & 31;
+          const int      leader = __ffs(ball) - 1;
+          unsigned       base   = 0;
+          if (lane == leader) base = atomicAdd(S.ovf_count, (unsigned)__popc(ball));
+          base = __shfl_sync(ball, base, leader);
+          S.ovf[base + __popc(ball & ((1u << lane) - 1u))] = (int32_t)p;
+          continue;
+        }
+      }
 #pragma unroll
       for (int d = 0; d < 3; ++d) q.u[d] = ux[d][p];
       real e0[3], b0[3];
       int  ic[3] = { q.i[0] + ng, q.i[1] + ng, D == 3 ? q.i[2] + ng : 0 };
       real dc[3] = { (real)q.dx[0], (real)q.dx[1], D == 3 ? (real)q.dx[2] : (real)0 };
-      if (near) {
-        if constexpr (O == 0) interp_zigzag<D, real>(ebv, ic, dc, e0, b0);
-        else                  interp_shape<D, O, real>(ebv, ic, dc, e0, b0);
-      } else {
-        // drifted past the margin: gather from global memory
-        if constexpr (O == 0) interp_zigzag<D, real>(a.EB, ic, dc, e0, b0);
-        else                  interp_shape<D, O, real>(a.EB, ic, dc, e0, b0);
-      }
+      if constexpr (O == 0) interp_zigzag<D, real>(ebv, ic, dc, e0, b0);
+      else                  interp_shape<D, O, real>(ebv, ic, dc, e0, b0);
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         e0[d] = e0[d] * a.dx;
@@ -310,15 +339,6 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
         }
       }
       if (q.tag == PIC_TAG_DEAD || S.charge == (real)0) continue;
-      if (edge || !near) {
-        // reference coordinates, global atomics
-        const FieldView<real>& J  = a.J;
-        const bool             ok = deposit_particle<D, O, real>(
-          q, w[p], S.charge, a.inv_dt, a.dx, ng, a.pc.ext,
-          [&](int i, int j, int k, int c, real v) { atomicAdd(J.p + J.idx(i, j, k, c), v); });
-        if (!ok) atomicAdd(a.err + ERR_STENCIL_OUT, 1ull);
-        continue;
-      }
       // deposit at the coordinates before the periodic wrap (a shift of both
       // i and i_prev by n leaves every contribution unchanged up to the image
       // cell, which the flush folds back)
@@ -327,12 +347,15 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
         q.i[d] -= q.wrap[d];
         q.ip[d] -= q.wrap[d];
       }
-      const int jb = -joff[0] - joff[1] * G::WJ0 - joff[2] * (G::WJ0 * G::WJ1);
-      deposit_particle<D, O, real>(q, w[p], S.charge, a.inv_dt, a.dx, ng, nullptr,
+      // in fixed point the weight carries the power-of-two scale, so every
+      // contribution arrives scaled exactly (w 2^s rounds like w)
+      const int  jb = -joff[0] - joff[1] * G::WJ0 - joff[2] * (G::WJ0 * G::WJ1);
+      const real wp = fixed ? w[p] * scale : w[p];
+      deposit_particle<D, O, real>(q, wp, S.charge, a.inv_dt, a.dx, ng, nullptr,
                                    [&](int i, int j, int k, int c, real v) {
                                      const int e = jb + i + j * G::WJ0 +
                                                    k * (G::WJ0 * G::WJ1) + c * G::NJ;
-                                     if (fixed) FA::add(Jw + e, G::PLANE, v, scale);
+                                     if (fixed) FA::add(Jw + e, G::PLANE, v);
                                      else       atomicAdd(Jr + e, v);
                                    });
     }
