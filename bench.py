@@ -42,11 +42,20 @@ WORKLOADS = {
     "turb3d": dict(name="3D SR decaying turbulence 256^3, e-/e+ 8 ppc each, order 2, "
                         "4 filter passes, FP32", dim=3, n=(256, 256, 256), order=2, ppc=8,
                    temp=0.09, drift=0.0, nfilter=4, cfl=0.45, skindepth0=10.0, larmor0=10.0,
-                   ppc0=16.0, modes=8, dB=1.0, sample_n=(64, 64, 64)),
+                   ppc0=16.0, field="turbulent", modes=8, dB=1.0, sample_n=(64, 64, 64),
+                   precision_n=(64, 64, 64), precision_steps=200),
     "pair2d": dict(name="2D SR pair plasma 512^2, e-/e+ 16 ppc each, drift +-0.3c, order 1, FP32",
                    dim=2, n=(512, 512, 1), order=1, ppc=16, temp=0.01, drift=0.3, nfilter=0,
-                   cfl=0.45, skindepth0=10.0, larmor0=10.0, ppc0=16.0, modes=0, dB=0.0,
-                   sample_n=(128, 128, 1)),
+                   cfl=0.45, skindepth0=10.0, larmor0=10.0, ppc0=16.0, field="none", modes=0,
+                   dB=0.0, sample_n=(128, 128, 1), precision_n=(512, 512, 1),
+                   precision_steps=100),
+    # magnetized uniform plasma: sigma = (skin depth / Larmor radius)^2 = 10,
+    # Maxwell-Juttner theta = 1, uniform B0 along x3
+    "sweep3d": dict(name="3D SR magnetized uniform plasma 192^3, e-/e+ 32 ppc each, sigma 10, "
+                         "theta 1, order 3, FP32 vs FP64", dim=3, n=(192, 192, 192), order=3,
+                    ppc=32, temp=1.0, drift=0.0, nfilter=0, cfl=0.45, skindepth0=10.0,
+                    larmor0=10.0 / math.sqrt(10.0), ppc0=64.0, field="uniform", modes=0, dB=0.0,
+                    sample_n=(24, 24, 24), precision_n=(192, 192, 192), precision_steps=1000),
 }
 
 # algorithmic bytes of the fused push+deposit, FP32: per particle read
@@ -54,6 +63,12 @@ WORKLOADS = {
 # the E/B gather (24 B) and the J flush (12 B)
 BYTES_PER_PARTICLE = {2: 32 + 28, 3: 40 + 36}
 BYTES_PER_CELL = 24 + 12
+
+# DRAM bytes (read + write) per particle of one k_push_deposit_tiled launch,
+# from an ncu capture of the same plasma on a 96^3 box (14,155,776 particles:
+# 637.1 MB read + 467.1 MB written); traffic grows with the particle count at
+# fixed particles per cell, so it scales to the full box by npart
+DRAM_BYTES_PER_PARTICLE = {"turb3d": 1104.1e6 / 14155776}
 
 
 def dist_env():
@@ -65,12 +80,13 @@ def dist_env():
 
 def make_setup(w, device, n=None):
     from entity_gb300.inputs import GridSpec, empty_field, make_species, turbulent_field
-    from entity_gb300.sim import step_params
     n = n or w["n"]
     g = GridSpec(dim=w["dim"], n=n, order=w["order"], real=torch.float32)
     B0 = 1.0 / w["larmor0"]
-    if w["modes"] > 0:
+    if w["field"] == "turbulent":
         EB = turbulent_field(g, B0, w["dB"], w["modes"], seed=2, device=device)
+    elif w["field"] == "uniform":
+        EB = turbulent_field(g, B0, 0.0, 0, seed=2, device=device)
     else:
         EB = empty_field(g, 6, device)
     J = empty_field(g, 3, device)
@@ -165,6 +181,76 @@ def cpu_sample(w, steps, warmup=1):
                        f"sort off"), "seconds": dt}
 
 
+def precision_twin(w, n, steps, sort_interval, every, timers=False, warm=0):
+    """FP32 and FP64 runs of the same plasma from identical initial states
+    (the FP32 inputs converted exactly to FP64), each through pic_srpic_step;
+    FP64 field energy and particle moments at checkpoints. Returns the error
+    of the FP32 run against the FP64 run and both throughputs."""
+    import dataclasses
+    from entity_gb300.inputs import empty_field
+    from entity_gb300.sim import Context
+    g32, EB32, J32, buff32, sp32 = make_setup(w, "cuda", n=n)
+    g64 = dataclasses.replace(g32, real=torch.float64)
+    EB64 = EB32.double()
+    J64, buff64 = empty_field(g64, 3, "cuda"), empty_field(g64, 3, "cuda")
+    sp64 = [s.astype(torch.float64) for s in sp32]
+    npart = sum(s.npart for s in sp32)
+    res = {}
+    for tag, (g, EB, J, buff, sp) in (("f64", (g64, EB64, J64, buff64, sp64)),
+                                      ("f32", (g32, EB32, J32, buff32, sp32))):
+        ctx = Context(g)
+        prm = step_prm(g, w, sort_interval)
+        series = []
+
+        def probe(k):
+            e2, b2 = ctx.field_energy(EB, g.dx)
+            m = ctx.particle_moments(sp)
+            series.append({"step": k, "field": e2 + b2, "kinetic": m[4], "mgamma": m[0],
+                           "p": m[1:4]})
+
+        probe(0)
+        evs = []
+        for k in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            if timers and k == warm:
+                ctx.timers(True)
+            a.record()
+            ctx.step(sp, EB, J, buff, prm, k)
+            b.record()
+            if k >= warm:
+                evs.append((a, b))
+            if (k + 1) % every == 0 or k + 1 == steps:
+                probe(k + 1)
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        res[tag] = {"series": series, "ms": ms,
+                    "value": npart * len(evs) / (ms / 1e3),
+                    "phases": ctx.read_timers() if timers else None,
+                    "errors": ctx.device_errors()}
+        ctx.close()
+    s32, s64 = res["f32"]["series"], res["f64"]["series"]
+    rel = lambda a, b: abs(a - b) / abs(b) if b != 0 else abs(a - b)
+    fe = [rel(a["field"], b["field"]) for a, b in zip(s32, s64)]
+    ke = [rel(a["kinetic"], b["kinetic"]) for a, b in zip(s32, s64)]
+    pe = [max(abs(x - y) for x, y in zip(a["p"], b["p"])) / b["mgamma"]
+          for a, b in zip(s32, s64)]
+    tot = lambda s: s["field"] + s["kinetic"]
+    return {
+        "steps": steps, "cells": list(n[:w["dim"]]), "particles": npart,
+        "field_energy_rel_err_final": fe[-1], "field_energy_rel_err_max": max(fe),
+        "kinetic_energy_rel_err_final": ke[-1], "kinetic_energy_rel_err_max": max(ke),
+        "momentum_err_rel_sum_m_gamma_max": max(pe),
+        "energy_drift_f32": rel(tot(s32[-1]), tot(s32[0])),
+        "energy_drift_f64": rel(tot(s64[-1]), tot(s64[0])),
+        "field_energy_f64_final": s64[-1]["field"], "field_energy_f64_initial": s64[0]["field"],
+        "checkpoint_every": every,
+        "f32_particle_steps_per_s": res["f32"]["value"],
+        "f64_particle_steps_per_s": res["f64"]["value"],
+        "device_errors": {"f32": res["f32"]["errors"], "f64": res["f64"]["errors"]},
+        "_phases_f32": res["f32"]["phases"], "_ms_f32": res["f32"]["ms"],
+    }
+
+
 def run_reference(args, w):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -247,6 +333,9 @@ def run_ours(args, w):
     bytes_pd = npart * BYTES_PER_PARTICLE[g.dim] + g.ncells() * BYTES_PER_CELL
     achieved = bytes_pd / (pd_ms / pd_n / 1e3) / 1e9
     peak, peak_src = hbm_peak()
+    traffic = None
+    if args.workload in DRAM_BYTES_PER_PARTICLE and not args.reference_sort_key:
+        traffic = DRAM_BYTES_PER_PARTICLE[args.workload] * npart
 
     # end to end through pic_srpic_step with host buffers: every step copies
     # the full particle and field state from pinned host memory and back
@@ -281,6 +370,14 @@ def run_ours(args, w):
 
     if rank != 0:
         return
+    # FP32 against FP64 on a sub-box of the same plasma from identical
+    # initial states: the error the FP32 throughput is quoted at
+    precision = None
+    psteps = w["precision_steps"] if args.precision_steps is None else args.precision_steps
+    if psteps > 0:
+        precision = precision_twin(w, w["precision_n"], psteps, args.sort_interval, every=50)
+        for k in [k for k in precision if k.startswith("_")]:
+            del precision[k]
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         cpu = cpu_sample(w, steps=args.cpu_steps)
@@ -296,12 +393,66 @@ def run_ours(args, w):
         "ns_per_particle_step": 1e9 / (value / world),
         "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in phases.items()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "kernel": "k_push_deposit (fused push + deposit, both species, J zero)",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "k_push_deposit_tiled (fused push + deposit, both species, "
+                               "plus the overflow-list drain)",
                      "bytes_per_launch": bytes_pd, "launch_ms": pd_ms / pd_n,
                      "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_src})"},
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "precision": precision,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_sweep(args, w):
+    """The FP32 vs FP64 precision sweep as its own line: both precisions run
+    the full workload for warmup + steps steps from identical initial states;
+    `value` is the FP32 throughput over the timed steps."""
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from __graft_entry__ import build
+    build()
+    from entity_gb300 import abi
+    lib = abi.load()
+    n = args.cells or w["n"]
+    total = args.warmup + args.steps
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = lib.pic_kernel_launches()
+    pr = precision_twin(w, n, total, args.sort_interval, every=args.checkpoint_every,
+                        timers=True, warm=args.warmup)
+    launches = lib.pic_kernel_launches() - launches0
+    clocks = sampler.stop()
+    phases = pr.pop("_phases_f32")
+    ms = pr.pop("_ms_f32")
+    value = pr["f32_particle_steps_per_s"]
+    npart = pr["particles"]
+    ncells = math.prod(n[:w["dim"]])
+    pd_ms, pd_n = phases["PushDeposit"]
+    bytes_pd = npart * BYTES_PER_PARTICLE[w["dim"]] + ncells * BYTES_PER_CELL
+    achieved = bytes_pd / (pd_ms / pd_n / 1e3) / 1e9
+    peak, peak_src = hbm_peak()
+    cpu = None if args.no_cpu_baseline else cpu_sample(w, steps=args.cpu_steps)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w["name"], "cells": ncells, "particles_per_gpu": npart,
+                   "sort_interval": args.sort_interval, "sort_key": "tile-major",
+                   "l2": "inputs larger than L2", "parallelism": "replicas x1"},
+        "ns_per_particle_step": 1e9 / value,
+        "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in phases.items()},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "k_push_deposit_tiled (FP32, both species)",
+                     "bytes_per_launch": bytes_pd, "launch_ms": pd_ms / pd_n,
+                     "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_src})"},
+        "precision": pr,
+        "cpu_baseline": cpu,
+        "e2e": None,
         "gpu_launches": launches,
         "clocks": clocks,
     }
@@ -324,6 +475,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision-steps", type=int, default=None,
+                    help="steps of the FP32-vs-FP64 twin on the sub-box (0 = skip)")
+    ap.add_argument("--checkpoint-every", type=int, default=50,
+                    help="steps between FP64 diagnostics in the precision sweep")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.cells is not None:
@@ -331,6 +486,8 @@ def main():
         args.cells = tuple(c)
     if args.impl == "reference":
         run_reference(args, w)
+    elif args.workload == "sweep3d":
+        run_sweep(args, w)
     else:
         run_ours(args, w)
 

@@ -12,6 +12,7 @@
 
 #include "../../include/entity_pic.h"
 #include "fields.cuh"
+#include "moments.cuh"
 #include "push_deposit_tiled.cuh"
 #include "sort.cuh"
 
@@ -60,7 +61,7 @@ struct pic_ctx {
   std::vector<SpeciesBins> bins;
   pic_grid             grid;
   unsigned long long*  d_err     = nullptr;  // 4 counters
-  double*              d_energy  = nullptr;  // 2
+  double*              d_energy  = nullptr;  // 2 field sums, then PIC_NMOMENTS
   // sort scratch (grown on demand)
   void*                sort_buf  = nullptr;
   size_t               sort_bytes = 0;
@@ -380,7 +381,7 @@ int pic_create(const pic_grid* grid, pic_ctx** out) {
   pic_ctx* c = new pic_ctx();
   c->grid    = *grid;
   if (cudaMalloc((void**)&c->d_err, sizeof(unsigned long long) * 4) != cudaSuccess ||
-      cudaMalloc((void**)&c->d_energy, sizeof(double) * 2) != cudaSuccess) {
+      cudaMalloc((void**)&c->d_energy, sizeof(double) * (2 + PIC_NMOMENTS)) != cudaSuccess) {
     if (c->d_err) cudaFree(c->d_err);
     delete c;
     return PIC_ERR_NOMEM;
@@ -674,6 +675,57 @@ int pic_field_energy(pic_ctx* c, const void* EB, double dx, double* out, void* s
   if (cudaMemcpyAsync(out, c->d_energy, sizeof(double) * 2, cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return PIC_ERR_CUDA;
   return cuda_status(cudaStreamSynchronize(s));
+}
+
+int pic_particle_moments(pic_ctx* c, const pic_species* sp, int32_t nspecies,
+                         double out[PIC_NMOMENTS], void* stream) {
+  if (!c || !out || nspecies < 0 || (nspecies > 0 && !sp)) return PIC_ERR_ARG;
+  for (int k = 0; k < nspecies; ++k) {
+    int st = validate_species(c, sp + k, false);
+    if (st != PIC_OK) return st;
+  }
+  cudaStream_t s = strm(stream);
+  double*      d = c->d_energy + 2;
+  if (cudaMemsetAsync(d, 0, sizeof(double) * PIC_NMOMENTS, s) != cudaSuccess) return PIC_ERR_CUDA;
+  for (int k = 0; k < nspecies; ++k) {
+    const pic::SpeciesPtrs p = sptrs(sp + k);
+    cudaError_t e = is_f64(c) ? pic::launch_particle_moments<double>(p, d, s)
+                              : pic::launch_particle_moments<float>(p, d, s);
+    if (e != cudaSuccess) return PIC_ERR_CUDA;
+  }
+  if (cudaMemcpyAsync(out, d, sizeof(double) * PIC_NMOMENTS, cudaMemcpyDeviceToHost, s) !=
+      cudaSuccess)
+    return PIC_ERR_CUDA;
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
+int pic_charge_density(pic_ctx* c, const pic_species* sp, int32_t nspecies, void* rho,
+                       void* stream) {
+  if (!c || !rho || nspecies < 0 || (nspecies > 0 && !sp)) return PIC_ERR_ARG;
+  for (int k = 0; k < nspecies; ++k) {
+    int st = validate_species(c, sp + k, false);
+    if (st != PIC_OK) return st;
+  }
+  pic::PushConsts pc{};
+  for (int d = 0; d < 3; ++d) {
+    pc.n[d]   = c->grid.n[d];
+    pc.ext[d] = d < c->grid.dim ? c->grid.n[d] + 2 * c->grid.ng : 1;
+  }
+  pc.ng          = c->grid.ng;
+  cudaStream_t s = strm(stream);
+  for (int k = 0; k < nspecies; ++k) {
+    if (sp[k].pusher == PIC_PUSHER_PHOTON || sp[k].charge == 0.0f) continue;
+    const pic::SpeciesPtrs p = sptrs(sp + k);
+    cudaError_t e =
+      is_f64(c) ? pic::launch_charge_density<double>(c->grid.dim, c->grid.order, p,
+                                                     cur_view<double>(c, rho), c->grid.ng, pc,
+                                                     c->d_err, s)
+                : pic::launch_charge_density<float>(c->grid.dim, c->grid.order, p,
+                                                    cur_view<float>(c, rho), c->grid.ng, pc,
+                                                    c->d_err, s);
+    if (e != cudaSuccess) return PIC_ERR_CUDA;
+  }
+  return PIC_OK;
 }
 
 int pic_get_device_errors(pic_ctx* c, int64_t out[4], int32_t reset, void* stream) {

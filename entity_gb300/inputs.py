@@ -88,6 +88,14 @@ class SpeciesArrays:
                              mv(self.u), self.w.to(device), self.tag.to(device), self.mass,
                              self.charge, self.pusher, self.npart, self.index)
 
+    def astype(self, real):
+        """A copy whose momenta and weights are converted to `real` (cells,
+        offsets and tags are shared as copies)."""
+        cl = lambda xs: [None if x is None else x.clone() for x in xs]
+        return SpeciesArrays(cl(self.i), cl(self.dx), cl(self.i_prev), cl(self.dx_prev),
+                             [x.to(real) for x in self.u], self.w.to(real), self.tag.clone(),
+                             self.mass, self.charge, self.pusher, self.npart, self.index)
+
     def clone(self):
         cl = lambda xs: [x.clone() for x in xs]
         return SpeciesArrays(cl(self.i), cl(self.dx), cl(self.i_prev), cl(self.dx_prev),

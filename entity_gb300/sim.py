@@ -146,6 +146,18 @@ class Context:
         abi.call("pic_field_energy", self.h, _ptr(EB), dx, out, _stream_ptr(stream))
         return out[0], out[1]
 
+    def particle_moments(self, species, stream=None):
+        """FP64 sums (m gamma, u1, u2, u3, w m (gamma - 1), w) over alive particles."""
+        arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
+        out = (C.c_double * 6)()
+        abi.call("pic_particle_moments", self.h, arr, len(species), out, _stream_ptr(stream))
+        return list(out)
+
+    def charge_density(self, species, rho, stream=None):
+        """Adds the deposit-consistent node charge density to rho[0] (J layout)."""
+        arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
+        abi.call("pic_charge_density", self.h, arr, len(species), _ptr(rho), _stream_ptr(stream))
+
     def device_errors(self, reset=False, stream=None):
         out = (C.c_int64 * 4)()
         abi.call("pic_get_device_errors", self.h, out, int(reset), _stream_ptr(stream))

@@ -224,6 +224,31 @@ int pic_field_energy(pic_ctx* ctx, const void* EB, double dx, double* out, void*
 int pic_field_energy_noalloc(const pic_grid* grid, const void* EB, double dx, double* out,
                              void* stream);
 
+/* FP64 particle moments over the alive particles of nspecies species, the
+ * SR Cartesian stress-energy sums of ReducedParticleMoments_kernel<SRPIC,
+ * Minkowski, T> (src/kernels/reduced_stats.hpp:403-538, unweighted as there):
+ * out[0] = sum m * gamma (sum |u| for massless), out[1..3] = sum u1, u2, u3;
+ * and out[4] = sum w * m * (gamma - 1), the weighted kinetic energy (|u| for
+ * massless), out[5] = sum w. The reference's normalisation (dV / (total
+ * volume * ppc0), metadomain_stats.cpp:113-116) is the caller's.
+ * Synchronises the stream. */
+#define PIC_NMOMENTS 6
+int pic_particle_moments(pic_ctx* ctx, const pic_species* sp, int32_t nspecies,
+                         double out[PIC_NMOMENTS], void* stream);
+
+/* Node charge density conserved by the current deposit: adds
+ * rho(n) += charge * w * prod_d S(n_d - x_d) for every alive particle into
+ * component 0 of `rho`, an array with the current layout (cur_stride), where
+ * S is the unstaggered shape of the grid's order (order 0, the zigzag
+ * deposit: the linear shape). Ghost nodes receive contributions like J and
+ * are folded by pic_sync_currents. With it the discrete continuity equation
+ * (rho_after - rho_before) / dt + D^- J = 0 holds node by node for one
+ * pic_deposit (D^- the backward difference of J's staggered components).
+ * The caller zeroes `rho`. No counterpart in the reference, whose Rho moment
+ * (particle_moments.hpp) smooths with its own window. */
+int pic_charge_density(pic_ctx* ctx, const pic_species* sp, int32_t nspecies, void* rho,
+                       void* stream);
+
 /* Device error word: out[0] = particles with an invalid tag seen by the
  * pusher, out[1] = alive particles whose cell lies outside the grid (skipped
  * by the pusher, reported by the sort), out[2] = particles whose deposit

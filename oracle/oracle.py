@@ -60,6 +60,8 @@ def lib(real):
         L.orc_field_energy.argtypes = [G, V, C.c_double, C.POINTER(C.c_double)]
         L.orc_kinetic_energy.restype = C.c_double
         L.orc_kinetic_energy.argtypes = [S]
+        L.orc_charge_density.argtypes = [G, S, V, C.c_int]
+        L.orc_particle_moments.argtypes = [S, C.POINTER(C.c_double)]
         L.orc_max_threads.restype = C.c_int
         L.orc_real_size.restype = C.c_int
         _libs[tag] = L
@@ -160,6 +162,20 @@ class Oracle:
     def kinetic_energy(self, sp):
         s = self.species(sp)
         return self.L.orc_kinetic_energy(C.byref(s))
+
+    def charge_density(self, species, rho):
+        for sp in species:
+            if sp.charge == 0.0:
+                continue
+            s = self.species(sp)
+            self.L.orc_charge_density(C.byref(self.og), C.byref(s), _p(rho), self.g.order)
+
+    def particle_moments(self, species):
+        out = (C.c_double * 6)()
+        for sp in species:
+            s = self.species(sp)
+            self.L.orc_particle_moments(C.byref(s), out)
+        return list(out)
 
     # the SR step sequence of SRPICEngine::step_forward (srpic.hpp:65-188)
     def step(self, species, EB, J, buff, prm, step, filter_passes=None):

@@ -1106,7 +1106,7 @@ void orc_sort_tiled(const orc_grid* g, orc_species* sp, const int* tile, int64_t
 
 int64_t orc_remove_dead(const orc_grid* g, orc_species* sp) {
   const int64_t np = sp->npart;
-  int64_t*      perm = (int64_t*)malloc(sizeof(int64_t) * (size_t)(np > 0 ? np : 1));
+  int64_t*      perm = (int64_t*)calloc((size_t)(np > 0 ? np : 1), sizeof(int64_t));
   int64_t       na   = 0;
   if (!perm) return np;
   for (int64_t p = 0; p < np; ++p)
@@ -1156,4 +1156,56 @@ double orc_kinetic_energy(const orc_species* sp) {
     s += (double)w[p] * (sqrt(1.0 + a * a + b * b + c * c) - 1.0) * (double)sp->mass;
   }
   return s;
+}
+
+void orc_charge_density(const orc_grid* g, const orc_species* sp, void* rho_, int order) {
+  real*       rho = (real*)rho_;
+  const real* w   = (const real*)sp->weight;
+  const int   O   = order == 0 ? 1 : order;
+  const int   ng  = g->ng;
+  const real  charge = (real)sp->charge;
+  for (int64_t p = 0; p < sp->npart; ++p) {
+    if (sp->tag[p] != ORC_TAG_ALIVE) continue;
+    int  imin[3] = { 0, 0, 0 };
+    real S[3][4];
+    shape(0, O, sp->i1[p], (real)sp->dx1[p], &imin[0], S[0]);
+    shape(0, O, sp->i2[p], (real)sp->dx2[p], &imin[1], S[1]);
+    if (g->dim == 3) shape(0, O, sp->i3[p], (real)sp->dx3[p], &imin[2], S[2]);
+    const real q = charge * w[p];
+    if (g->dim == 2) {
+      for (int j = 0; j <= O; ++j) {
+        const real qj = q * S[1][j];
+        for (int i = 0; i <= O; ++i)
+          rho[JI(g, imin[0] + ng + i, imin[1] + ng + j, 0, 0)] += qj * S[0][i];
+      }
+    } else {
+      for (int k = 0; k <= O; ++k)
+        for (int j = 0; j <= O; ++j) {
+          const real qjk = q * S[2][k] * S[1][j];
+          for (int i = 0; i <= O; ++i)
+            rho[JI(g, imin[0] + ng + i, imin[1] + ng + j, imin[2] + ng + k, 0)] +=
+              qjk * S[0][i];
+        }
+    }
+  }
+}
+
+void orc_particle_moments(const orc_species* sp, double* out) {
+  const real*  u1 = (const real*)sp->ux1;
+  const real*  u2 = (const real*)sp->ux2;
+  const real*  u3 = (const real*)sp->ux3;
+  const real*  w  = (const real*)sp->weight;
+  const double m  = (double)sp->mass;
+  for (int64_t p = 0; p < sp->npart; ++p) {
+    if (sp->tag[p] != ORC_TAG_ALIVE) continue;
+    const double a = u1[p], b = u2[p], c = u3[p];
+    const double u2s = a * a + b * b + c * c;
+    const double gm  = sqrt(1.0 + u2s);
+    out[0] += m == 0.0 ? sqrt(u2s) : m * gm;
+    out[1] += a;
+    out[2] += b;
+    out[3] += c;
+    out[4] += (double)w[p] * (m == 0.0 ? sqrt(u2s) : m * (u2s / (gm + 1.0)));
+    out[5] += (double)w[p];
+  }
 }

@@ -129,6 +129,18 @@ void orc_field_energy(const orc_grid* g, const void* EB, double dx, double* out)
 /* sum over particles of w * (gamma - 1) * mass (in FP64) */
 double orc_kinetic_energy(const orc_species* sp);
 
+/* node charge density conserved by the deposit, added into component 0 of a
+ * current-layout array: rho(n) += charge * w * prod_d S(n_d - x_d) with the
+ * unstaggered shape of the given order (order 0: the linear shape); the
+ * discrete form of the continuity equation that Esirkepov's weights
+ * (currents_deposit.hpp:406-754) and the zigzag fluxes satisfy */
+void orc_charge_density(const orc_grid* g, const orc_species* sp, void* rho, int order);
+
+/* FP64 particle moments over alive particles (reduced_stats.hpp:403-538,
+ * SR Cartesian T components, unweighted): out[0] += sum m gamma,
+ * out[1..3] += sum u_i, out[4] += sum w m (gamma - 1), out[5] += sum w */
+void orc_particle_moments(const orc_species* sp, double* out);
+
 #ifdef __cplusplus
 }
 #endif
