@@ -51,6 +51,12 @@ WORKLOADS = {
                    precision_steps=100),
     # magnetized uniform plasma: sigma = (skin depth / Larmor radius)^2 = 10,
     # Maxwell-Juttner theta = 1, uniform B0 along x3
+    # two cold beams at +-0.2c (16 ppc each) with weights 1 + 1e-3 cos(k x),
+    # k = 2 pi / L; gradient of the final E energy after 400 steps
+    "adjoint2d": dict(name="2D two-stream adjoint 256^2, cold beams +-0.2c, 16 ppc each, "
+                           "amplitude 1e-3, order 2, FP32, 400 steps, checkpoint every 20",
+                      dim=2, n=(256, 256, 1), order=2, ppc=16, beta=0.2, amp=1e-3,
+                      skindepth0=10.0, cfl=0.45, steps=400, every=20),
     "sweep3d": dict(name="3D SR magnetized uniform plasma 192^3, e-/e+ 32 ppc each, sigma 10, "
                          "theta 1, order 3, FP32 vs FP64", dim=3, n=(192, 192, 192), order=3,
                     ppc=32, temp=1.0, drift=0.0, nfilter=0, cfl=0.45, skindepth0=10.0,
@@ -407,6 +413,103 @@ def run_ours(args, w):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args, w):
+    """Adjoint/forward cost and gradient checks on the two-stream problem."""
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from __graft_entry__ import build
+    build()
+    from entity_gb300 import abi
+    from entity_gb300 import adjoint as A
+    from entity_gb300.sim import Context
+    lib = abi.load()
+    nsteps = args.adjoint_steps or w["steps"]
+    every = args.checkpoint_every or w["every"]
+    n = (args.cells or w["n"])[:2]
+
+    def setup(real):
+        g, prm, kappa, k = A.two_stream(n=n, ppc_per_beam=w["ppc"], order=w["order"], real=real,
+                                        skindepth0=w["skindepth0"], cfl=w["cfl"])
+        return g, prm, kappa, k, Context(g)
+
+    def grads(real, timed=False):
+        g, prm, kappa, k, ctx = setup(real)
+        beta = torch.tensor(w["beta"], dtype=torch.float64, device="cuda", requires_grad=True)
+        amp = torch.tensor(w["amp"], dtype=torch.float64, device="cuda", requires_grad=True)
+        sp, U, W, EB0 = A.build(g, kappa, k, beta, amp, w["ppc"], ctx)
+        out = {"particles": sum(s.npart for s in sp)}
+        if timed:
+            # warm-up, then the plain forward and the full gradient, both timed
+            A.forward_energy(ctx, g, prm, sp, U, W, EB0, min(nsteps, 5))
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            l0 = lib.pic_kernel_launches()
+            e0.record()
+            out["L_forward"] = A.forward_energy(ctx, g, prm, sp, U, W, EB0, nsteps)
+            e1.record()
+            torch.cuda.synchronize()
+            out["forward_ms"] = e0.elapsed_time(e1)
+            out["forward_launches"] = lib.pic_kernel_launches() - l0
+            e0.record()
+        L = A.energy(ctx, g, prm, sp, U, W, EB0, nsteps, every)
+        gb, ga = torch.autograd.grad(L, [beta, amp])
+        if timed:
+            e1.record()
+            torch.cuda.synchronize()
+            out["gradient_ms"] = e0.elapsed_time(e1)
+        out.update(L=float(L.detach()), dL_dbeta=float(gb), dL_damp=float(ga))
+        return out
+
+    def fd(real, which, h):
+        g, prm, kappa, k, ctx = setup(real)
+        vals = []
+        for sgn in (1, -1):
+            b = w["beta"] + (sgn * h if which == "beta" else 0.0)
+            a = w["amp"] + (sgn * h if which == "amp" else 0.0)
+            sp, U, W, EB0 = A.build(g, kappa, k, torch.tensor(b, dtype=torch.float64, device="cuda"),
+                                    torch.tensor(a, dtype=torch.float64, device="cuda"), w["ppc"],
+                                    ctx)
+            vals.append(A.forward_energy(ctx, g, prm, sp, U, W, EB0, nsteps))
+        return (vals[0] - vals[1]) / (2 * h)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    r32 = grads(torch.float32, timed=True)
+    clocks = sampler.stop()
+    r64 = grads(torch.float64)
+    rel = lambda a, b: abs(a - b) / abs(b) if b != 0 else abs(a - b)
+    # central differences at h = 1e-4, and for the drift also at 2e-3: the
+    # float in-cell offsets round every position each step (~3e-8 cells,
+    # coherently across a cold beam), which a 1e-4 drift change over 400
+    # steps resolves only to ~1e-3
+    checks = {"h": 1e-4, "h_drift_large": 2e-3}
+    for real, tag, r in ((torch.float32, "f32", r32), (torch.float64, "f64", r64)):
+        fb, fa, fb2 = fd(real, "beta", 1e-4), fd(real, "amp", 1e-4), fd(real, "beta", 2e-3)
+        checks[tag] = {"dL_dbeta": r["dL_dbeta"], "fd_dbeta": fb,
+                       "rel_err_dbeta": rel(r["dL_dbeta"], fb),
+                       "fd_dbeta_h2e-3": fb2, "rel_err_dbeta_h2e-3": rel(r["dL_dbeta"], fb2),
+                       "dL_damp": r["dL_damp"], "fd_damp": fa, "rel_err_damp": rel(r["dL_damp"], fa)}
+    checks["f32_vs_f64"] = {"rel_err_dbeta": rel(r32["dL_dbeta"], r64["dL_dbeta"]),
+                            "rel_err_damp": rel(r32["dL_damp"], r64["dL_damp"]),
+                            "rel_err_L": rel(r32["L"], r64["L"])}
+    npart = r32["particles"]
+    value = npart * nsteps / (r32["forward_ms"] / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": nsteps,
+        "warmup": min(nsteps, 5), "ms_per_step": r32["forward_ms"] / nsteps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": w["name"], "cells": n[0] * n[1], "particles_per_gpu": npart,
+                   "checkpoint_every": every, "sort_interval": 0, "parallelism": "replicas x1"},
+        "adjoint": {"ratio_gradient_to_forward": r32["gradient_ms"] / r32["forward_ms"],
+                    "forward_ms": r32["forward_ms"], "gradient_ms": r32["gradient_ms"],
+                    "L": r32["L"], "L_forward": r32["L_forward"], "checks": checks},
+        "gpu_launches": r32["forward_launches"],
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_sweep(args, w):
     """The FP32 vs FP64 precision sweep as its own line: both precisions run
     the full workload for warmup + steps steps from identical initial states;
@@ -422,7 +525,7 @@ def run_sweep(args, w):
     sampler = ClockSampler(local)
     sampler.start()
     launches0 = lib.pic_kernel_launches()
-    pr = precision_twin(w, n, total, args.sort_interval, every=args.checkpoint_every,
+    pr = precision_twin(w, n, total, args.sort_interval, every=args.checkpoint_every or 50,
                         timers=True, warm=args.warmup)
     launches = lib.pic_kernel_launches() - launches0
     clocks = sampler.stop()
@@ -477,8 +580,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision-steps", type=int, default=None,
                     help="steps of the FP32-vs-FP64 twin on the sub-box (0 = skip)")
-    ap.add_argument("--checkpoint-every", type=int, default=50,
-                    help="steps between FP64 diagnostics in the precision sweep")
+    ap.add_argument("--checkpoint-every", type=int, default=None,
+                    help="steps between FP64 diagnostics (sweep3d, default 50) or between "
+                         "adjoint checkpoints (adjoint2d, default 20)")
+    ap.add_argument("--adjoint-steps", type=int, default=None,
+                    help="forward steps of the adjoint workload (default 400)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.cells is not None:
@@ -488,6 +594,8 @@ def main():
         run_reference(args, w)
     elif args.workload == "sweep3d":
         run_sweep(args, w)
+    elif args.workload == "adjoint2d":
+        run_adjoint(args, w)
     else:
         run_ours(args, w)
 

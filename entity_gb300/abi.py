@@ -71,6 +71,10 @@ class PicSpecies(C.Structure):
     ]
 
 
+class PicSpeciesAdjoint(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("lx1", "lx2", "lx3", "lu1", "lu2", "lu3", "lw")]
+
+
 class PicStepParams(C.Structure):
     _fields_ = [
         ("dt", C.c_double), ("dx", C.c_double), ("omegaB0", C.c_double),
@@ -116,6 +120,20 @@ SIGNATURES = {
     "pic_charge_density": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32, _VP, _VP]),
     "pic_srpic_step": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32, _VP, _VP, _VP,
                                  C.POINTER(PicStepParams), C.c_int64, _VP]),
+    "pic_checkpoint_save": (C.c_int, [_VP, C.c_int32, C.POINTER(PicSpecies), C.c_int32, _VP,
+                                      _VP]),
+    "pic_checkpoint_restore": (C.c_int, [_VP, C.c_int32, C.POINTER(PicSpecies), C.c_int32,
+                                         _VP, _VP]),
+    "pic_checkpoint_release": (C.c_int, [_VP]),
+    "pic_checkpoint_view": (C.c_int, [_VP, C.c_int32, C.POINTER(PicSpecies), C.c_int32,
+                                      C.POINTER(PicSpecies), C.POINTER(_VP)]),
+    "pic_field_energy_adjoint_seed": (C.c_int, [_VP, _VP, _VP, C.c_double, _VP]),
+    "pic_srpic_step_adjoint": (C.c_int, [_VP, C.POINTER(PicSpecies),
+                                         C.POINTER(PicSpeciesAdjoint), C.c_int32, _VP, _VP,
+                                         C.POINTER(PicStepParams), _VP]),
+    "pic_srpic_gradient": (C.c_int, [_VP, C.POINTER(PicSpecies), C.POINTER(PicSpeciesAdjoint),
+                                     C.c_int32, _VP, _VP, _VP, C.POINTER(PicStepParams),
+                                     C.c_int64, C.c_int64, _VP, C.POINTER(C.c_double), _VP]),
     "pic_timers_enable": (C.c_int, [_VP, C.c_int32]),
     "pic_timers_reset": (C.c_int, [_VP]),
     "pic_timers_read": (C.c_int, [_VP, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),

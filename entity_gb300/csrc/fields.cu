@@ -556,6 +556,202 @@ cudaError_t launch_energy(const GridInfo& g, FieldView<real> EB, double dx, doub
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// adjoint (transposed) field operators. Each forward update of the step is a
+// periodic linear map on the active cells (ghosts hold images); its transpose
+// is applied in gather form to a ghost-filled adjoint field. Yee stencils only.
+// ---------------------------------------------------------------------------
+
+// lam(active, c < 3) = 2 h_c dV E_c: the gradient of the E part of the FP64
+// energy of k_energy with respect to E; lam(active, c >= 3) = 0
+template <int D, typename real>
+__global__ void k_adj_seed(CellIter it, FieldView<real> EB, FieldView<real> lam, double dx) {
+  const double  dV     = D == 3 ? dx * dx * dx : dx * dx;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < it.count; t += stride) {
+    int i1, i2, i3;
+    it.cell(t, i1, i2, i3);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double h = (c < D) ? dx * dx : 1.0;
+      lam.p[lam.idx(i1, i2, i3, c)] = (real)(2.0 * h * dV * (double)EB.p[EB.idx(i1, i2, i3, c)]);
+      lam.p[lam.idx(i1, i2, i3, c + 3)] = (real)0;
+    }
+  }
+}
+
+// transpose of CurrentsAmpere's E += jcoeff * J: lamJ = jcoeff * lamE at the
+// active cells and their images
+template <int D, typename real>
+__global__ void k_adj_currents(GridInfo g, CellIter it, FieldView<real> lam, FieldView<real> lamJ,
+                               real jcoeff) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < it.count; t += stride) {
+    int i1, i2, i3;
+    it.cell(t, i1, i2, i3);
+    real v[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      v[c]                              = jcoeff * lam.p[lam.idx(i1, i2, i3, c)];
+      lamJ.p[lamJ.idx(i1, i2, i3, c)] = v[c];
+    }
+    for_images<D>(g, i1, i2, i3, [&](int a, int b, int e) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) lamJ.p[lamJ.idx(a, b, e, c)] = v[c];
+    });
+  }
+}
+
+// transpose of k_ampere's curl: lamB(active) += A^T lamE (lamE ghost-filled)
+template <int D, typename real>
+__global__ void k_adj_ampere(CellIter it, FieldView<real> lam, real a1, real a2) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < it.count; t += stride) {
+    int i, j, k;
+    it.cell(t, i, j, k);
+#define L(a, b, c, comp) lam.p[lam.idx(a, b, c, comp)]
+    if constexpr (D == 2) {
+      L(i, j, 0, 5) += a1 * (L(i, j, 0, 0) - L(i, j + 1, 0, 0)) + a1 * (L(i + 1, j, 0, 1) - L(i, j, 0, 1));
+      L(i, j, 0, 3) += a2 * (L(i, j + 1, 0, 2) - L(i, j, 0, 2));
+      L(i, j, 0, 4) += a2 * (L(i, j, 0, 2) - L(i + 1, j, 0, 2));
+    } else {
+      L(i, j, k, 3) += a1 * (L(i, j, k, 1) - L(i, j, k + 1, 1)) + a1 * (L(i, j + 1, k, 2) - L(i, j, k, 2));
+      L(i, j, k, 4) += a1 * (L(i, j, k + 1, 0) - L(i, j, k, 0)) + a1 * (L(i, j, k, 2) - L(i + 1, j, k, 2));
+      L(i, j, k, 5) += a1 * (L(i, j, k, 0) - L(i, j + 1, k, 0)) + a1 * (L(i + 1, j, k, 1) - L(i, j, k, 1));
+    }
+#undef L
+  }
+}
+
+// transpose of k_faraday (Yee): lamE(active) += F^T lamB (lamB ghost-filled)
+template <int D, typename real>
+__global__ void k_adj_faraday(CellIter it, FieldView<real> lam, real c1, real c2) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < it.count; t += stride) {
+    int i, j, k;
+    it.cell(t, i, j, k);
+#define L(a, b, c, comp) lam.p[lam.idx(a, b, c, comp)]
+    if constexpr (D == 2) {
+      L(i, j, 0, 2) += c1 * (L(i, j, 0, 3) - L(i, j - 1, 0, 3)) + c1 * (L(i - 1, j, 0, 4) - L(i, j, 0, 4));
+      L(i, j, 0, 0) += c2 * (L(i, j - 1, 0, 5) - L(i, j, 0, 5));
+      L(i, j, 0, 1) += c2 * (L(i, j, 0, 5) - L(i - 1, j, 0, 5));
+    } else {
+      L(i, j, k, 0) += c1 * (L(i, j, k, 4) - L(i, j, k - 1, 4)) + c1 * (L(i, j - 1, k, 5) - L(i, j, k, 5));
+      L(i, j, k, 1) += c1 * (L(i, j, k - 1, 3) - L(i, j, k, 3)) + c1 * (L(i, j, k, 5) - L(i - 1, j, k, 5));
+      L(i, j, k, 2) += c1 * (L(i, j, k, 3) - L(i, j - 1, k, 3)) + c1 * (L(i - 1, j, k, 4) - L(i, j, k, 4));
+    }
+#undef L
+  }
+}
+
+// transpose of the ghost fill: every active cell adds the values its ghost
+// images accumulated (components [c0, c1)) and clears them
+template <int D, typename real>
+__global__ void k_adj_fold(GridInfo g, CellIter it, FieldView<real> f, int c0, int c1) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < it.count; t += stride) {
+    int i1, i2, i3;
+    it.cell(t, i1, i2, i3);
+    if (!near_periodic_edge(g, D, i1, i2, i3)) continue;
+    // each ghost cell is the image of exactly one active cell, so the
+    // thread that folds it may also clear it
+    for (int c = c0; c < c1; ++c) {
+      real acc = 0;
+      for_images<D>(g, i1, i2, i3, [&](int a, int b, int e) {
+        real* q = f.p + f.idx(a, b, e, c);
+        acc += *q;
+        *q = (real)0;
+      });
+      f.p[f.idx(i1, i2, i3, c)] += acc;
+    }
+  }
+}
+
+// zero the ghost cells of components [c0, c1)
+template <typename real>
+__global__ void k_zero_ghosts(GridInfo g, FieldView<real> f, int c0, int c1) {
+  const int     e0 = g.n[0] + 2 * g.ng, e1 = g.n[1] + 2 * g.ng;
+  const int     e2 = g.dim == 3 ? g.n[2] + 2 * g.ng : 1;
+  const int64_t count  = (int64_t)e0 * e1 * e2;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += stride) {
+    int64_t   r = t;
+    const int i = (int)(r % e0);
+    r /= e0;
+    const int j = (int)(r % e1);
+    const int k = (int)(r / e1);
+    const bool ghost = i < g.ng || i >= g.n[0] + g.ng || j < g.ng || j >= g.n[1] + g.ng ||
+                       (g.dim == 3 && (k < g.ng || k >= g.n[2] + g.ng));
+    if (!ghost) continue;
+    for (int c = c0; c < c1; ++c) f.p[f.idx(i, j, k, c)] = (real)0;
+  }
+}
+
+template <typename real>
+cudaError_t launch_adj_seed(const GridInfo& g, FieldView<real> EB, FieldView<real> lam, double dx,
+                            cudaStream_t s) {
+  const CellIter it = make_iter(g);
+  if (g.dim == 2) PIC_KL(k_adj_seed<2, real><<<grid_for(it.count, 256), 256, 0, s>>>(it, EB, lam, dx));
+  else            PIC_KL(k_adj_seed<3, real><<<grid_for(it.count, 256), 256, 0, s>>>(it, EB, lam, dx));
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_adj_currents(const GridInfo& g, FieldView<real> lam, FieldView<real> lamJ,
+                                real jcoeff, cudaStream_t s) {
+  const CellIter it = make_iter(g);
+  if (g.dim == 2) PIC_KL(k_adj_currents<2, real><<<grid_for(it.count, 256), 256, 0, s>>>(g, it, lam, lamJ, jcoeff));
+  else            PIC_KL(k_adj_currents<3, real><<<grid_for(it.count, 256), 256, 0, s>>>(g, it, lam, lamJ, jcoeff));
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_adj_ampere(const GridInfo& g, FieldView<real> lam, real a1, real a2,
+                              cudaStream_t s) {
+  const CellIter it = make_iter(g);
+  if (g.dim == 2) PIC_KL(k_adj_ampere<2, real><<<grid_for(it.count, 256), 256, 0, s>>>(it, lam, a1, a2));
+  else            PIC_KL(k_adj_ampere<3, real><<<grid_for(it.count, 256), 256, 0, s>>>(it, lam, a1, a2));
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_adj_faraday(const GridInfo& g, FieldView<real> lam, real c1, real c2,
+                               cudaStream_t s) {
+  const CellIter it = make_iter(g);
+  if (g.dim == 2) PIC_KL(k_adj_faraday<2, real><<<grid_for(it.count, 256), 256, 0, s>>>(it, lam, c1, c2));
+  else            PIC_KL(k_adj_faraday<3, real><<<grid_for(it.count, 256), 256, 0, s>>>(it, lam, c1, c2));
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_adj_fold(const GridInfo& g, FieldView<real> f, int c0, int c1, cudaStream_t s) {
+  const CellIter it = make_iter(g);
+  if (g.dim == 2) PIC_KL(k_adj_fold<2, real><<<grid_for(it.count, 256), 256, 0, s>>>(g, it, f, c0, c1));
+  else            PIC_KL(k_adj_fold<3, real><<<grid_for(it.count, 256), 256, 0, s>>>(g, it, f, c0, c1));
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_zero_ghosts(const GridInfo& g, FieldView<real> f, int c0, int c1,
+                               cudaStream_t s) {
+  const int64_t cells = (int64_t)(g.n[0] + 2 * g.ng) * (g.n[1] + 2 * g.ng) *
+                        (g.dim == 3 ? g.n[2] + 2 * g.ng : 1);
+  PIC_KL(k_zero_ghosts<real><<<grid_for(cells, 256), 256, 0, s>>>(g, f, c0, c1));
+  return cudaGetLastError();
+}
+
+#define PIC_INST_ADJ_FIELDS(R)                                                                     \
+  template cudaError_t launch_adj_seed<R>(const GridInfo&, FieldView<R>, FieldView<R>, double,     \
+                                          cudaStream_t);                                           \
+  template cudaError_t launch_adj_currents<R>(const GridInfo&, FieldView<R>, FieldView<R>, R,      \
+                                              cudaStream_t);                                       \
+  template cudaError_t launch_adj_ampere<R>(const GridInfo&, FieldView<R>, R, R, cudaStream_t);    \
+  template cudaError_t launch_adj_faraday<R>(const GridInfo&, FieldView<R>, R, R, cudaStream_t);   \
+  template cudaError_t launch_adj_fold<R>(const GridInfo&, FieldView<R>, int, int, cudaStream_t);  \
+  template cudaError_t launch_zero_ghosts<R>(const GridInfo&, FieldView<R>, int, int, cudaStream_t);
+PIC_INST_ADJ_FIELDS(float)
+PIC_INST_ADJ_FIELDS(double)
+
 #define PIC_INST_FIELDS(R)                                                                       \
   template cudaError_t launch_faraday<R>(const GridInfo&, FieldView<R>, R, R, const Stencil<R>&, \
                                          bool, cudaStream_t);                                    \

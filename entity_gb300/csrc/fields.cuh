@@ -41,4 +41,24 @@ template <typename real>
 cudaError_t launch_energy(const GridInfo& g, FieldView<real> EB, double dx, double* out,
                           cudaStream_t s);
 
+
+// adjoint (transposed) field operators, Yee stencils (fields.cu)
+template <typename real>
+cudaError_t launch_adj_seed(const GridInfo& g, FieldView<real> EB, FieldView<real> lam, double dx,
+                            cudaStream_t s);
+template <typename real>
+cudaError_t launch_adj_currents(const GridInfo& g, FieldView<real> lam, FieldView<real> lamJ,
+                                real jcoeff, cudaStream_t s);
+template <typename real>
+cudaError_t launch_adj_ampere(const GridInfo& g, FieldView<real> lam, real a1, real a2,
+                              cudaStream_t s);
+template <typename real>
+cudaError_t launch_adj_faraday(const GridInfo& g, FieldView<real> lam, real c1, real c2,
+                               cudaStream_t s);
+template <typename real>
+cudaError_t launch_adj_fold(const GridInfo& g, FieldView<real> f, int c0, int c1, cudaStream_t s);
+template <typename real>
+cudaError_t launch_zero_ghosts(const GridInfo& g, FieldView<real> f, int c0, int c1,
+                               cudaStream_t s);
+
 }  // namespace pic

@@ -83,7 +83,7 @@ class SpeciesArrays:
     index: int = 1
 
     def to(self, device):
-        mv = lambda xs: [x.to(device) for x in xs]
+        mv = lambda xs: [None if x is None else x.to(device) for x in xs]
         return SpeciesArrays(mv(self.i), mv(self.dx), mv(self.i_prev), mv(self.dx_prev),
                              mv(self.u), self.w.to(device), self.tag.to(device), self.mass,
                              self.charge, self.pusher, self.npart, self.index)
@@ -97,7 +97,7 @@ class SpeciesArrays:
                              self.mass, self.charge, self.pusher, self.npart, self.index)
 
     def clone(self):
-        cl = lambda xs: [x.clone() for x in xs]
+        cl = lambda xs: [None if x is None else x.clone() for x in xs]
         return SpeciesArrays(cl(self.i), cl(self.dx), cl(self.i_prev), cl(self.dx_prev),
                              cl(self.u), self.w.clone(), self.tag.clone(), self.mass,
                              self.charge, self.pusher, self.npart, self.index)

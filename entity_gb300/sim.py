@@ -26,6 +26,25 @@ def _stream_ptr(stream):
     return C.c_void_p(stream.cuda_stream)
 
 
+class SpeciesAdjoint:
+    """Adjoint arrays of one species (pic_species_adjoint): gradients with
+    respect to positions (per simulated axis), momenta and weights."""
+
+    def __init__(self, g: GridSpec, npart: int, device="cuda"):
+        z = lambda: torch.zeros(max(npart, 1), dtype=g.real, device=device)
+        self.lx = [z() for _ in range(g.dim)]
+        self.lu = [z() for _ in range(3)]
+        self.lw = z()
+
+    def c(self) -> abi.PicSpeciesAdjoint:
+        a = abi.PicSpeciesAdjoint()
+        a.lx1, a.lx2 = self.lx[0].data_ptr(), self.lx[1].data_ptr()
+        a.lx3 = self.lx[2].data_ptr() if len(self.lx) > 2 else None
+        a.lu1, a.lu2, a.lu3 = (t.data_ptr() for t in self.lu)
+        a.lw = self.lw.data_ptr()
+        return a
+
+
 def make_grid(g: GridSpec) -> abi.PicGrid:
     pg = abi.PicGrid()
     pg.dim = g.dim
@@ -162,6 +181,44 @@ class Context:
         out = (C.c_int64 * 4)()
         abi.call("pic_get_device_errors", self.h, out, int(reset), _stream_ptr(stream))
         return list(out)
+
+    # --- adjoint ----------------------------------------------------------------
+    def gradient(self, species, adjoints, EB, J, buff, prm: abi.PicStepParams, nsteps,
+                 checkpoint_every, lamEB, stream=None):
+        """Gradient of the final E-field energy after nsteps with respect to the
+        initial state (pic_srpic_gradient); returns the energy. `adjoints` is
+        one SpeciesAdjoint per species; species and EB end at the initial state."""
+        arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
+        adj = (abi.PicSpeciesAdjoint * len(adjoints))(*[a.c() for a in adjoints])
+        loss = C.c_double(0)
+        abi.call("pic_srpic_gradient", self.h, arr, adj, len(species), _ptr(EB), _ptr(J),
+                 _ptr(buff), C.byref(prm), nsteps, checkpoint_every, _ptr(lamEB),
+                 C.byref(loss), _stream_ptr(stream))
+        for k, s in enumerate(species):
+            s.npart = arr[k].npart
+        return loss.value
+
+    def step_adjoint(self, species, adjoints, EB, lamEB, prm: abi.PicStepParams, stream=None):
+        arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
+        adj = (abi.PicSpeciesAdjoint * len(adjoints))(*[a.c() for a in adjoints])
+        abi.call("pic_srpic_step_adjoint", self.h, arr, adj, len(species), _ptr(EB), _ptr(lamEB),
+                 C.byref(prm), _stream_ptr(stream))
+
+    def energy_adjoint_seed(self, EB, lamEB, dx, stream=None):
+        abi.call("pic_field_energy_adjoint_seed", self.h, _ptr(EB), _ptr(lamEB), dx,
+                 _stream_ptr(stream))
+
+    def checkpoint_save(self, slot, species, EB, stream=None):
+        arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
+        abi.call("pic_checkpoint_save", self.h, slot, arr, len(species), _ptr(EB),
+                 _stream_ptr(stream))
+
+    def checkpoint_restore(self, slot, species, EB, stream=None):
+        arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
+        abi.call("pic_checkpoint_restore", self.h, slot, arr, len(species), _ptr(EB),
+                 _stream_ptr(stream))
+        for k, s in enumerate(species):
+            s.npart = arr[k].npart
 
     # --- phase timers ---------------------------------------------------------
     def timers(self, on=True):

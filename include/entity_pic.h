@@ -301,6 +301,75 @@ typedef struct {
 int pic_srpic_step(pic_ctx* ctx, pic_species* sp, int32_t nspecies, void* EB, void* J,
                    void* buff, const pic_step_params* prm, int64_t step, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Adjoint (reverse mode) of the SR step. No counterpart in the reference.
+ *
+ * Scope: 2D Cartesian grids, periodic fields and particles, Boris pusher
+ * (pusher NONE species are carried along untouched), shape orders 1-3, Yee
+ * solver, any number of filter passes. Positions are differentiated as
+ * continuous coordinates X = i + dx, so orders >= 2 give an almost
+ * everywhere smooth gradient.
+ * ------------------------------------------------------------------------ */
+
+/* Adjoint arrays of one species, real_t, at least npart long: the gradient
+ * with respect to the position along each simulated axis (lx3 unused in 2D),
+ * to the three momentum components, and to the weight. */
+typedef struct {
+  void* lx1;
+  void* lx2;
+  void* lx3;
+  void* lu1;
+  void* lu2;
+  void* lu3;
+  void* lw;
+} pic_species_adjoint;
+
+/* Checkpoint store inside the context. A slot holds EB and, per species, the
+ * arrays a step changes (cells, offsets, momenta, tags); weights are not
+ * copied. Slots are allocated on first use and kept until
+ * pic_checkpoint_release or pic_destroy. Stream-ordered. */
+int pic_checkpoint_save(pic_ctx* ctx, int32_t slot, const pic_species* sp, int32_t nspecies,
+                        const void* EB, void* stream);
+/* Restores a slot into the given arrays and npart (same species count). */
+int pic_checkpoint_restore(pic_ctx* ctx, int32_t slot, pic_species* sp, int32_t nspecies,
+                           void* EB, void* stream);
+/* Species descriptors (copies of `like` with their state arrays pointing
+ * into the slot) and the slot's EB, for reading a saved state in place. */
+int pic_checkpoint_view(pic_ctx* ctx, int32_t slot, const pic_species* like, int32_t nspecies,
+                        pic_species* out, void** EB);
+int pic_checkpoint_release(pic_ctx* ctx);
+
+/* lamEB = d/dEB of the E part of pic_field_energy (out[0]): 2 h dV E on the
+ * active cells, zero elsewhere (ghosts included). */
+int pic_field_energy_adjoint_seed(pic_ctx* ctx, const void* EB, void* lamEB, double dx,
+                                  void* stream);
+
+/* One step backwards. Given the state at the start of step n (species
+ * arrays and EB, ghosts need not be filled) and the adjoint of the state at
+ * the start of step n + 1 (adj arrays and lamEB, an EB-shaped array whose
+ * ghosts are zero), overwrites them with the adjoint of the state at the
+ * start of step n; adj.lw accumulates. The step is the one pic_srpic_step
+ * takes with `prm` (sort and dead removal are not differentiated: the
+ * caller runs the forward with both off). */
+int pic_srpic_step_adjoint(pic_ctx* ctx, const pic_species* sp, pic_species_adjoint* adj,
+                           int32_t nspecies, const void* EB, void* lamEB,
+                           const pic_step_params* prm, void* stream);
+
+/* Gradient of the final E-field energy (pic_field_energy out[0]) after
+ * `nsteps` forward steps with respect to the initial state: runs the
+ * forward from the given state with a checkpoint every `checkpoint_every`
+ * steps (sort and dead removal off), then each segment backwards,
+ * recomputing its steps from its checkpoint. On return *loss holds the
+ * energy, adj the gradients with respect to the initial positions, momenta
+ * and weights, lamEB the gradient with respect to the initial E and B, and
+ * the species and EB arrays hold the initial state again. Memory: about
+ * (nsteps / checkpoint_every + checkpoint_every) copies of the particle
+ * state. Synchronises the stream. */
+int pic_srpic_gradient(pic_ctx* ctx, pic_species* sp, pic_species_adjoint* adj,
+                       int32_t nspecies, void* EB, void* J, void* buff,
+                       const pic_step_params* prm, int64_t nsteps, int64_t checkpoint_every,
+                       void* lamEB, double* loss, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
