@@ -1,6 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles oracle/srpic_oracle.c twice with gcc into oracle/_build/:
+Compiles oracle/srpic_oracle.c and oracle/grpic_oracle.c twice with gcc into
+oracle/_build/:
   liboracle_f32.so  (real = float,  the reference's SINGLE_PRECISION build)
   liboracle_f64.so  (real = double)
 with -ffp-contract=off so every operation is rounded as written, and OpenMP so
@@ -13,7 +14,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
 
-SOURCES = ["srpic_oracle.c"]
+SOURCES = ["srpic_oracle.c", "grpic_oracle.c"]
 FLAGS = ["-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
          "-fopenmp", "-Wall", "-Wno-unused-function"]
 
@@ -27,7 +28,8 @@ def _stale(target, deps):
 
 def build(verbose=False):
     os.makedirs(OUT, exist_ok=True)
-    deps = [os.path.join(HERE, s) for s in SOURCES] + [os.path.join(HERE, "srpic_oracle.h")]
+    deps = [os.path.join(HERE, s) for s in SOURCES] + [
+        os.path.join(HERE, h) for h in ("srpic_oracle.h", "grpic_oracle.h", "grpic_metric.inc")]
     libs = {}
     for tag, defs in (("f32", ["-DORC_SINGLE"]), ("f64", [])):
         target = os.path.join(OUT, f"liboracle_{tag}.so")

@@ -5,6 +5,7 @@ module, as the checker. Arrays are CPU torch tensors in the same layout as the
 GPU path (see entity_gb300/inputs.py).
 """
 import ctypes as C
+import math
 import os
 
 import torch
@@ -220,3 +221,109 @@ class Oracle:
                 self.remove_dead(sp)
             if prm.sort_interval > 0 and step % prm.sort_interval == 0:
                 self.sort(sp)
+
+
+# ---------------------------------------------------------------------------
+# GR (QKerrSchild) oracle, grpic_oracle.h
+# ---------------------------------------------------------------------------
+class OrcQKS(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("a", "rh", "r0", "h", "chi_min", "eta_min", "dchi",
+                                          "deta", "dchi_inv", "deta_inv")] + [
+        ("small_angle", C.c_int)]
+
+
+GR_NQ = 24
+GR_NAMES = ["h_11", "h_22", "h_33", "h_13", "h11", "h22", "h33", "h13", "alpha", "beta1",
+            "sqrt_det_h", "sqrt_det_h_tilde", "dr_alpha", "dt_alpha", "dr_beta1", "dt_beta1",
+            "dr_h11", "dr_h22", "dr_h33", "dr_h13", "dt_h11", "dt_h22", "dt_h33", "dt_h13"]
+
+
+def _gr_sigs(L):
+    if getattr(L, "_gr_ready", False):
+        return L
+    V, D = C.c_void_p, C.c_double
+    Q, G, S = C.POINTER(OrcQKS), C.POINTER(OrcGrid), C.POINTER(OrcSpecies)
+    I2 = C.c_int * 2
+    L.orc_qks_init.argtypes = [Q, C.c_int, C.c_int, D, D, D, D, D, D, D]
+    L.orc_gr_metric.argtypes = [Q, V, C.c_int64, V]
+    L.orc_gr_transform.argtypes = [Q, C.c_int, V, V, C.c_int64, V]
+    L.orc_gr_push.argtypes = [G, Q, S, V, V, D, D, C.c_int, C.c_int, I2, I2, C.c_int]
+    L.orc_gr_deposit.argtypes = [G, Q, S, V, D, C.c_int]
+    L.orc_gr_faraday.argtypes = [G, Q, V, V, V, D, C.c_int]
+    L.orc_gr_ampere.argtypes = [G, Q, V, V, V, D, C.c_int, C.c_int]
+    L.orc_gr_currents_ampere.argtypes = [G, Q, V, V, D, C.c_int, C.c_int]
+    L.orc_gr_aux_e.argtypes = [G, Q, V, V, V, C.c_int]
+    L.orc_gr_aux_h.argtypes = [G, Q, V, V, V, C.c_int]
+    L.orc_gr_average_db.argtypes = [G, V, V]
+    L.orc_gr_average_j.argtypes = [G, V, V]
+    L.orc_gr_field_bcs.argtypes = [G, V, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+    L._gr_ready = True
+    return L
+
+
+class GROracle(Oracle):
+    """The reference's GR kernels on the CPU for one (r, theta) grid."""
+
+    def __init__(self, g, a, r_min, r_max, th_min=0.0, th_max=math.pi, r0=0.0, h=0.0):
+        super().__init__(g)
+        _gr_sigs(self.L)
+        self.q = OrcQKS()
+        self.L.orc_qks_init(C.byref(self.q), g.n[0], g.n[1], r_min, r_max, th_min, th_max, a,
+                            r0, h)
+
+    def metric(self, x):
+        x = torch.as_tensor(x, dtype=torch.float64).contiguous()
+        n = x.shape[0]
+        out = torch.empty((n, GR_NQ), dtype=torch.float64)
+        self.L.orc_gr_metric(C.byref(self.q), _p(x), n, _p(out))
+        return {k: out[:, j] for j, k in enumerate(GR_NAMES)}
+
+    def transform(self, kind, x, v):
+        x = torch.as_tensor(x, dtype=torch.float64).contiguous()
+        v = torch.as_tensor(v, dtype=torch.float64).contiguous()
+        out = torch.empty_like(v)
+        self.L.orc_gr_transform(C.byref(self.q), kind, _p(x), _p(v), x.shape[0], _p(out))
+        return out
+
+    def gr_push(self, sp, em, em0, dt, omegaB0, niter=10, absorb=(1, 1), axis=(1, 1),
+                island_i1=0):
+        s = self.species(sp)
+        self.L.orc_gr_push(C.byref(self.og), C.byref(self.q), C.byref(s), _p(em), _p(em0), dt,
+                           omegaB0, niter, self.g.order, (C.c_int * 2)(*absorb),
+                           (C.c_int * 2)(*axis), island_i1)
+
+    def gr_deposit(self, species, J, dt, island_i1=0, zero=True):
+        if zero:
+            J.zero_()
+        for sp in species:
+            s = self.species(sp)
+            self.L.orc_gr_deposit(C.byref(self.og), C.byref(self.q), C.byref(s), _p(J), dt,
+                                  island_i1)
+
+    def gr_faraday(self, Bin, Bout, E, coeff, axis_min=1):
+        self.L.orc_gr_faraday(C.byref(self.og), C.byref(self.q), _p(Bin), _p(Bout), _p(E), coeff,
+                              axis_min)
+
+    def gr_ampere(self, Din, Dout, H, coeff, axis_min=1, axis_max=1):
+        self.L.orc_gr_ampere(C.byref(self.og), C.byref(self.q), _p(Din), _p(Dout), _p(H), coeff,
+                             axis_min, axis_max)
+
+    def gr_currents_ampere(self, D, J, coeff, axis_min=1, axis_max=1):
+        self.L.orc_gr_currents_ampere(C.byref(self.og), C.byref(self.q), _p(D), _p(J), coeff,
+                                      axis_min, axis_max)
+
+    def gr_aux_e(self, D, B, E, axis_max=1):
+        self.L.orc_gr_aux_e(C.byref(self.og), C.byref(self.q), _p(D), _p(B), _p(E), axis_max)
+
+    def gr_aux_h(self, D, B, H, axis_max=1):
+        self.L.orc_gr_aux_h(C.byref(self.og), C.byref(self.q), _p(D), _p(B), _p(H), axis_max)
+
+    def gr_average_db(self, f, f0):
+        self.L.orc_gr_average_db(C.byref(self.og), _p(f), _p(f0))
+
+    def gr_average_j(self, J, J0):
+        self.L.orc_gr_average_j(C.byref(self.og), _p(J), _p(J0))
+
+    def gr_field_bcs(self, fld, set_e, set_b, axis_min=1, axis_max=1, horizon=1, nfilter=0):
+        self.L.orc_gr_field_bcs(C.byref(self.og), _p(fld), int(set_e), int(set_b), axis_min,
+                                axis_max, horizon, nfilter)

@@ -487,7 +487,7 @@ int64_t orc_push(const orc_grid* g, orc_species* sp, const void* EBv, int order,
 /* current deposition: src/kernels/currents_deposit.hpp:108-761              */
 /* ------------------------------------------------------------------------ */
 static void deposit_one(const orc_grid* g, const orc_species* sp, real* J,
-                        int O, real inv_dt, real dx, int64_t p) {
+                        int O, real inv_dt, real dx, int64_t p, const real* vz) {
   const real* ux1 = (const real*)sp->ux1;
   const real* ux2 = (const real*)sp->ux2;
   const real* ux3 = (const real*)sp->ux3;
@@ -505,6 +505,8 @@ static void deposit_one(const orc_grid* g, const orc_species* sp, real* J,
   vp[0] *= inv_energy;
   vp[1] *= inv_energy;
   vp[2] *= inv_energy;
+  /* a caller-supplied out-of-plane velocity (the GR deposit's metric one) */
+  if (vz) vp[2] = vz[p];
   const real coeff = w[p] * (real)sp->charge;
   const int  ip[3] = { sp->i1_prev[p], sp->i2_prev[p], D == 3 ? sp->i3_prev[p] : 0 };
   const int  ic[3] = { sp->i1[p], sp->i2[p], D == 3 ? sp->i3[p] : 0 };
@@ -653,8 +655,34 @@ static void deposit_one(const orc_grid* g, const orc_species* sp, real* J,
   }
 }
 
+static void deposit_all(const orc_grid* g, const orc_species* sp, void* Jv, int order,
+                        double dt_d, double dx_d, const real* vz);
+
 void orc_deposit(const orc_grid* g, const orc_species* sp, void* Jv, int order,
                  double dt_d, double dx_d) {
+  deposit_all(g, sp, Jv, order, dt_d, dx_d, NULL);
+}
+
+void orc_deposit_vz(const orc_grid* g, const orc_species* sp, void* Jv, int order, double dt_d,
+                    const void* vz) {
+  deposit_all(g, sp, Jv, order, dt_d, 1.0, (const real*)vz);
+}
+
+void orc_interp2(const orc_grid* g, const void* emD, const void* emB, int order, int i1, int i2,
+                 float dx1, float dx2, double* e, double* b) {
+  const int  ic[3] = { i1, i2, 0 };
+  const real dc[3] = { (real)dx1, (real)dx2, ZERO };
+  real       e0[3], b0[3], e1[3], b1[3];
+  interp_shape(g, (const real*)emD, order, ic, dc, e0, b0);
+  interp_shape(g, (const real*)emB, order, ic, dc, e1, b1);
+  for (int c = 0; c < 3; ++c) {
+    e[c] = (double)e0[c];
+    b[c] = (double)b1[c];
+  }
+}
+
+static void deposit_all(const orc_grid* g, const orc_species* sp, void* Jv, int order,
+                        double dt_d, double dx_d, const real* vz) {
   real*      J      = (real*)Jv;
   const real inv_dt = ONE / (real)dt_d;
   const real dx     = (real)dx_d;
@@ -673,7 +701,7 @@ void orc_deposit(const orc_grid* g, const orc_species* sp, void* Jv, int order,
 #pragma omp for schedule(static)
       for (int64_t p = 0; p < sp->npart; ++p) {
         if (sp->tag[p] == ORC_TAG_DEAD) continue;
-        deposit_one(g, sp, Jt, order, inv_dt, dx, p);
+        deposit_one(g, sp, Jt, order, inv_dt, dx, p, vz);
       }
 #pragma omp for schedule(static)
       for (int64_t q = 0; q < nJ; ++q) {
@@ -688,7 +716,7 @@ void orc_deposit(const orc_grid* g, const orc_species* sp, void* Jv, int order,
 #endif
   for (int64_t p = 0; p < sp->npart; ++p) {
     if (sp->tag[p] == ORC_TAG_DEAD) continue;
-    deposit_one(g, sp, J, order, inv_dt, dx, p);
+    deposit_one(g, sp, J, order, inv_dt, dx, p, vz);
   }
 }
 

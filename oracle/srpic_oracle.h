@@ -126,6 +126,17 @@ int64_t orc_remove_dead(const orc_grid* g, orc_species* sp);
  * Minkowski): out[0] = sum E^2 dV-weighted, out[1] = sum B^2. */
 void orc_field_energy(const orc_grid* g, const void* EB, double dx, double* out);
 
+/* the deposit with a caller-supplied out-of-plane velocity vz[p] (real) in
+ * place of the SR one (the GR deposit, currents_deposit.hpp:138-165) */
+void orc_deposit_vz(const orc_grid* g, const orc_species* sp, void* J, int order, double dt,
+                    const void* vz);
+
+/* shape-order interpolation (sr.hpp:1151-1369) at a 2D particle position of
+ * the E part of emD and the B part of emB (gr.hpp:594-662 reads D from em and
+ * B from em0) */
+void orc_interp2(const orc_grid* g, const void* emD, const void* emB, int order, int i1, int i2,
+                 float dx1, float dx2, double* e, double* b);
+
 /* sum over particles of w * (gamma - 1) * mass (in FP64) */
 double orc_kinetic_energy(const orc_species* sp);
 

@@ -1,0 +1,115 @@
+"""Pins the GR oracle (QKerrSchild metric and transforms) to the reference's
+own metric tests.
+
+tests/metrics/ks-qks.cpp:185-197 builds QKerrSchild on a 32 x 42 grid over
+r in [0.8, 10], theta in [0, pi] with r0 = -2, h = 0, a = 0.8, and checks at
+every cell centre that h^ij and h_ij, converted to the physical basis
+(transform U -> PU and D -> PD, qkerr_schild.h:735-760), equal the analytic
+Kerr-Schild components, to 10 machine epsilons. The same comparison runs here
+against the analytic expressions evaluated in FP64. The metric derivatives
+the GR pusher uses are checked against central differences of the oracle's
+own metric functions (the alternative the reference keeps commented out in
+gr.hpp:286-305), and the vector transforms against the invariance of
+u_i u^i between the covariant and tetrad bases.
+"""
+import math
+
+import pytest
+import torch
+
+from entity_gb300.inputs import GridSpec
+from oracle.oracle import GROracle
+
+REALS = [torch.float32, torch.float64]
+EPS = {torch.float32: 1.1920929e-07, torch.float64: 2.220446049250313e-16}
+
+
+def _qks(real, n=(32, 42), a=0.8, r0=-2.0, rmin=0.8, rmax=10.0):
+    g = GridSpec(dim=2, n=(n[0], n[1], 1), order=1, real=real)
+    return GROracle(g, a=a, r_min=rmin, r_max=rmax, r0=r0), g
+
+
+def _centres(n):
+    i = torch.arange(n[0], dtype=torch.float64) + 0.5
+    j = torch.arange(n[1], dtype=torch.float64) + 0.5
+    I, Jm = torch.meshgrid(i, j, indexing="ij")
+    return torch.stack([I.reshape(-1), Jm.reshape(-1)], 1)
+
+
+@pytest.mark.parametrize("real", REALS)
+def test_qks_metric_matches_kerr_schild(real):
+    o, g = _qks(real)
+    q = o.q
+    x = _centres((32, 42))
+    m = o.metric(x)
+    chi = x[:, 0] * q.dchi + q.chi_min
+    r = q.r0 + torch.exp(chi)
+    th = x[:, 1] * q.deta + q.eta_min
+    a = q.a
+    S = r * r + (a * torch.cos(th)) ** 2
+    z = 2 * r / S
+    Dl = r * r - 2 * r + a * a
+    A = (r * r + a * a) ** 2 - (a * torch.sin(th)) ** 2 * Dl
+    s2 = torch.sin(th) ** 2
+    # physical-basis factors of transform<U, PU> / <D, PD> (h = 0)
+    fr = torch.exp(chi) * q.dchi
+    ft = q.deta
+    expect = {
+        "h11": (m["h11"] * fr * fr, A / (S * (S + 2 * r))),
+        "h22": (m["h22"] * ft * ft, 1 / S),
+        "h33": (m["h33"], 1 / (S * s2)),
+        "h13": (m["h13"] * fr, a / S),
+        "h_11": (m["h_11"] / (fr * fr), 1 + z),
+        "h_22": (m["h_22"] / (ft * ft), S),
+        "h_33": (m["h_33"], A * s2 / S),
+        "h_13": (m["h_13"] / fr, -a * (1 + z) * s2),
+        "alpha": (m["alpha"], 1 / torch.sqrt(1 + z)),
+        "beta1": (m["beta1"] * fr, z / (1 + z)),
+        "sqrt_det_h": (m["sqrt_det_h"] / (fr * ft), S * torch.sin(th) * torch.sqrt(1 + z)),
+    }
+    # the FP32 oracle evaluates exp/sin/cos in float from float coordinates
+    # (near the poles sin(theta) carries the rounding of theta itself);
+    # the FP64 expectation is exact to rounding, so allow a few tens of eps
+    tol = (100 if real == torch.float32 else 10) * EPS[real]
+    for k, (got, want) in expect.items():
+        rel = ((got - want).abs() / want.abs()).max()
+        assert float(rel) <= tol, (k, float(rel))
+
+
+def test_qks_derivatives_match_central_differences():
+    o, g = _qks(torch.float64)
+    x = _centres((32, 42))
+    x = x[(x[:, 1] > 2) & (x[:, 1] < 40)]  # away from the poles
+    m = o.metric(x)
+    h = 1e-5
+    for d, tag in ((0, "dr"), (1, "dt")):
+        xp, xm = x.clone(), x.clone()
+        xp[:, d] += h
+        xm[:, d] -= h
+        mp, mm = o.metric(xp), o.metric(xm)
+        for f in ("alpha", "beta1", "h11", "h22", "h33", "h13"):
+            fd = (mp[f] - mm[f]) / (2 * h)
+            an = m[f"{tag}_{f}"]
+            scale = float(an.abs().max()) + 1e-300
+            err = float((fd - an).abs().max()) / scale
+            assert err < 1e-6, (tag, f, err)
+
+
+@pytest.mark.parametrize("real", REALS)
+def test_transforms_preserve_the_norm(real):
+    o, g = _qks(real, a=0.95, r0=0.0, rmin=1.2, rmax=50.0, n=(64, 48))
+    x = _centres((64, 48))
+    x = x[(x[:, 1] > 1) & (x[:, 1] < 47)]
+    gen = torch.Generator().manual_seed(1)
+    v = torch.rand((x.shape[0], 3), generator=gen, dtype=torch.float64) * 2 - 1
+    vc = o.transform(0, x, v)      # covariant -> contravariant
+    vt = o.transform(2, x, v)      # covariant -> tetrad
+    back = o.transform(3, x, vt)   # tetrad -> covariant
+    n_cov = (v * vc).sum(1)
+    n_tet = (vt * vt).sum(1)
+    tol = 200 * EPS[real]
+    assert float(((n_cov - n_tet).abs() / n_tet.abs()).max()) < tol
+    assert float(((back - v).abs()).max()) < tol * 10
+    # contravariant -> tetrad of u^i equals covariant -> tetrad of u_i
+    vt2 = o.transform(1, x, vc)
+    assert float(((vt2 - vt).abs()).max()) < tol * 10
