@@ -57,6 +57,15 @@ WORKLOADS = {
                            "amplitude 1e-3, order 2, FP32, 400 steps, checkpoint every 20",
                       dim=2, n=(256, 256, 1), order=2, ppc=16, beta=0.2, amp=1e-3,
                       skindepth0=10.0, cfl=0.45, steps=400, every=20),
+    # Kerr (a = 0.95) quasi-spherical Kerr-Schild grid, r log-spaced in
+    # [0.9 r_h, 50 r_g], theta in [0, pi], vertical seed field, e-/e+ at rest
+    # 4 per cell in r < 6 r_g; FP32 with the pusher in FP64 within 3 cells of
+    # the horizon
+    "wald2d": dict(name="2D GR Wald problem 1024(r) x 512(theta), a 0.95, vertical field, "
+                        "e-/e+ 4 ppc in r < 6, order 2, FP32 with FP64 near the horizon",
+                   dim=2, n=(1024, 512, 1), order=2, a=0.95, r_max=50.0, ppc=4, r_inject=6.0,
+                   cfl=0.5, skindepth0=0.05, larmor0=0.0025, ppc0=2.0, niter=10,
+                   sort_interval=0, clear_interval=100),
     "sweep3d": dict(name="3D SR magnetized uniform plasma 192^3, e-/e+ 32 ppc each, sigma 10, "
                          "theta 1, order 3, FP32 vs FP64", dim=3, n=(192, 192, 192), order=3,
                     ppc=32, temp=1.0, drift=0.0, nfilter=0, cfl=0.45, skindepth0=10.0,
@@ -510,6 +519,63 @@ def run_adjoint(args, w):
     print(json.dumps(line), flush=True)
 
 
+def run_wald(args, w):
+    """GR step throughput on the Wald problem (pic_grpic_step)."""
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from __graft_entry__ import build
+    build()
+    from entity_gb300 import abi
+    from entity_gb300.gr import gr_step_params, horizon_island, wald_setup
+    lib = abi.load()
+    n = (args.cells or w["n"])[:2]
+    g, spec, ctx, fields, species = wald_setup(n=n, a=w["a"], r_max=w["r_max"], order=w["order"],
+                                               ppc=w["ppc"], r_inject=w["r_inject"])
+    prm = gr_step_params(ctx, cfl=w["cfl"], ppc0=w["ppc0"], skindepth0=w["skindepth0"],
+                         larmor0=w["larmor0"], sort_interval=w["sort_interval"],
+                         clear_interval=w["clear_interval"])
+    island = horizon_island(g, spec)
+    npart0 = sum(s.npart for s in species)
+    for k in range(args.warmup):
+        ctx.grpic_step(species, fields, prm, niter=w["niter"], island_i1=island, step=k)
+    torch.cuda.synchronize()
+    ctx.timers(True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    l0 = lib.pic_kernel_launches()
+    ev = []
+    steps_particles = 0
+    for k in range(args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        steps_particles += sum(s.npart for s in species)
+        a.record()
+        ctx.grpic_step(species, fields, prm, niter=w["niter"], island_i1=island,
+                       step=args.warmup + k)
+        b.record()
+        ev.append((a, b))
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = lib.pic_kernel_launches() - l0
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    phases = ctx.read_timers()
+    errs = ctx.device_errors()
+    value = steps_particles / (ms / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w["name"], "cells": n[0] * n[1], "particles_initial": npart0,
+                   "particles_final": sum(s.npart for s in species), "dt": prm.dt,
+                   "fp64_island_i1": island, "parallelism": "replicas x1"},
+        "ns_per_particle_step": 1e9 / value,
+        "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in phases.items()},
+        "device_errors": errs,
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_sweep(args, w):
     """The FP32 vs FP64 precision sweep as its own line: both precisions run
     the full workload for warmup + steps steps from identical initial states;
@@ -596,6 +662,8 @@ def main():
         run_sweep(args, w)
     elif args.workload == "adjoint2d":
         run_adjoint(args, w)
+    elif args.workload == "wald2d":
+        run_wald(args, w)
     else:
         run_ours(args, w)
 

@@ -75,6 +75,17 @@ class PicSpeciesAdjoint(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("lx1", "lx2", "lx3", "lu1", "lu2", "lu3", "lw")]
 
 
+class PicGRMetric(C.Structure):
+    _fields_ = [("a", C.c_double), ("r0", C.c_double), ("h", C.c_double),
+                ("x1min", C.c_double), ("x1max", C.c_double),
+                ("x2min", C.c_double), ("x2max", C.c_double),
+                ("axis_min", C.c_int32), ("axis_max", C.c_int32), ("horizon", C.c_int32)]
+
+
+class PicGRParams(C.Structure):
+    _fields_ = [("niter", C.c_int32), ("island_i1", C.c_int32)]
+
+
 class PicStepParams(C.Structure):
     _fields_ = [
         ("dt", C.c_double), ("dx", C.c_double), ("omegaB0", C.c_double),
@@ -134,6 +145,25 @@ SIGNATURES = {
     "pic_srpic_gradient": (C.c_int, [_VP, C.POINTER(PicSpecies), C.POINTER(PicSpeciesAdjoint),
                                      C.c_int32, _VP, _VP, _VP, C.POINTER(PicStepParams),
                                      C.c_int64, C.c_int64, _VP, C.POINTER(C.c_double), _VP]),
+    "pic_gr_metric_eval": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, C.c_int64, _VP, _VP]),
+    "pic_gr_push": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.POINTER(PicSpecies), _VP, _VP,
+                              C.c_double, C.c_double, C.c_int32, C.c_int32, _VP]),
+    "pic_gr_deposit": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.POINTER(PicSpecies), C.c_int32,
+                                 _VP, C.c_double, C.c_int32, C.c_uint32, _VP]),
+    "pic_gr_faraday": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP, _VP, C.c_double, _VP]),
+    "pic_gr_ampere": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP, _VP, C.c_double, _VP]),
+    "pic_gr_currents_ampere": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP, C.c_double,
+                                         _VP]),
+    "pic_gr_aux": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.c_int32, _VP, _VP, _VP, _VP]),
+    "pic_gr_average": (C.c_int, [_VP, C.c_int32, _VP, _VP, _VP]),
+    "pic_gr_field_bcs": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, C.c_int32, C.c_int32,
+                                   C.c_int32, _VP]),
+    "pic_gr_init_vertical": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP]),
+    "pic_gr_min_cell_size": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.POINTER(C.c_double),
+                                       _VP]),
+    "pic_grpic_step": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.POINTER(PicSpecies), C.c_int32,
+                                 C.POINTER(_VP), C.POINTER(PicStepParams),
+                                 C.POINTER(PicGRParams), C.c_int64, _VP]),
     "pic_timers_enable": (C.c_int, [_VP, C.c_int32]),
     "pic_timers_reset": (C.c_int, [_VP]),
     "pic_timers_read": (C.c_int, [_VP, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),

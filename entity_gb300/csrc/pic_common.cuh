@@ -433,18 +433,16 @@ __device__ __forceinline__ void move_and_bound(Prtl<real>& q, bool massive, real
 // than the ghost layers allow, i.e. a time step beyond the CFL limit);
 // ext == nullptr skips the check (the caller guarantees the window).
 template <int D, int O, typename real, typename Add>
+__device__ __forceinline__ bool deposit_with_velocity(const Prtl<real>& q, const real* vp,
+                                                      real weight, real charge, real inv_dt,
+                                                      int ng, const int* ext, Add&& add);
+
+template <int D, int O, typename real, typename Add>
 __device__ __forceinline__ bool deposit_particle(const Prtl<real>& q, real weight, real charge,
                                                  real inv_dt, real dx, int ng, const int* ext,
                                                  Add&& add) {
-  const real ONE = 1, HALF = 0.5, INV_2 = 0.5, ZERO = 0;
-  if constexpr (O == 0) {
-    if (ext) {
-#pragma unroll
-      for (int a = 0; a < D; ++a) {
-        if (min(q.ip[a], q.i[a]) + ng < 0 || max(q.ip[a], q.i[a]) + ng + 1 >= ext[a]) return false;
-      }
-    }
-  }
+  const real ONE = 1, ZERO = 0;
+  // Cartesian velocity for the unsimulated direction (currents_deposit.hpp:130-165)
   real       vp[3];
   vp[0] = q.u[0] / dx;
   vp[1] = q.u[1] / dx;
@@ -454,6 +452,24 @@ __device__ __forceinline__ bool deposit_particle(const Prtl<real>& q, real weigh
   vp[0] *= inv_energy;
   vp[1] *= inv_energy;
   vp[2] *= inv_energy;
+  return deposit_with_velocity<D, O, real>(q, vp, weight, charge, inv_dt, ng, ext, add);
+}
+
+// the deposit proper, given the particle velocity vp (the GR deposit passes
+// its metric velocity, currents_deposit.hpp:138-159)
+template <int D, int O, typename real, typename Add>
+__device__ __forceinline__ bool deposit_with_velocity(const Prtl<real>& q, const real* vp,
+                                                      real weight, real charge, real inv_dt,
+                                                      int ng, const int* ext, Add&& add) {
+  const real ONE = 1, HALF = 0.5, INV_2 = 0.5;
+  if constexpr (O == 0) {
+    if (ext) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        if (min(q.ip[a], q.i[a]) + ng < 0 || max(q.ip[a], q.i[a]) + ng + 1 >= ext[a]) return false;
+      }
+    }
+  }
   const real coeff = weight * charge;
 
   if constexpr (O == 0) {

@@ -370,6 +370,105 @@ int pic_srpic_gradient(pic_ctx* ctx, pic_species* sp, pic_species_adjoint* adj,
                        const pic_step_params* prm, int64_t nsteps, int64_t checkpoint_every,
                        void* lamEB, double* loss, void* stream);
 
+/* ------------------------------------------------------------------------
+ * GR: 2D quasi-spherical Kerr-Schild grids (metric::QKerrSchild<Dim::_2D>,
+ * src/metrics/qkerr_schild.h). The grid's axis 1 is the radial code
+ * coordinate (log-spaced r), axis 2 the polar one (theta). Fields are
+ * 6-component arrays with the em layout: D (or the auxiliary E) in 0..2, B
+ * (or the auxiliary H) in 3..5; currents use the cur layout. Particle
+ * boundaries come from pic_grid.prtl_bc: PIC_BC_ABSORB in r, PIC_BC_AXIS in
+ * theta. Only h = 0 (theta = eta) is supported.
+ * ------------------------------------------------------------------------ */
+typedef struct {
+  double  a;              /* spin, 0 <= a < 1 */
+  double  r0, h;          /* qsph_r0, qsph_h (h must be 0) */
+  double  x1min, x1max;   /* r extent (r_g) */
+  double  x2min, x2max;   /* theta extent */
+  int32_t axis_min;       /* field AXIS boundary at theta = x2min */
+  int32_t axis_max;       /* field AXIS boundary at theta = x2max */
+  int32_t horizon;        /* field HORIZON boundary at r = x1min */
+} pic_gr_metric;
+
+/* metric functions at n code-coordinate points x (device, n x 2 doubles);
+ * out (device, n x PIC_GR_NQ doubles): h_11 h_22 h_33 h_13 h11 h22 h33 h13
+ * alpha beta1 sqrt_det_h sqrt_det_h_tilde dr_alpha dt_alpha dr_beta1
+ * dt_beta1 dr_h11 dr_h22 dr_h33 dr_h13 dt_h11 dt_h22 dt_h33 dt_h13, in the
+ * grid's real_t */
+#define PIC_GR_NQ 24
+int pic_gr_metric_eval(pic_ctx* ctx, const pic_gr_metric* m, const double* x, int64_t n,
+                       double* out, void* stream);
+
+/* kernel::gr::Pusher_kernel (src/kernels/pushers/gr.hpp:664-865) for one
+ * species: D interpolated from em, B from em0 at the grid's shape order
+ * (1-3); Boris (massive) or photon; `niter` implicit iterations; prev arrays
+ * written. In a single-precision build, particles with i1 < island_i1 run
+ * the metric and both implicit iterations in double. The reference's
+ * UpdatePhi takes phi by value (gr.hpp:459-480), so phi is never changed
+ * there; it is not written here either. */
+int pic_gr_push(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, const void* em,
+                const void* em0, double dt, double omegaB0, int32_t niter, int32_t island_i1,
+                void* stream);
+
+/* grpic::CurrentsDeposit (src/engines/grpic/currents.h:29-73): the current
+ * of the last push at shape order 1 (hard-wired in the reference) with the
+ * metric out-of-plane velocity (currents_deposit.hpp:138-159); J is zeroed
+ * first unless flags has PIC_PD_NO_ZERO. */
+int pic_gr_deposit(pic_ctx* ctx, const pic_gr_metric* m, const pic_species* sp,
+                   int32_t nspecies, void* J, double dt, int32_t island_i1, uint32_t flags,
+                   void* stream);
+
+/* gr::Faraday_kernel (faraday_gr.hpp:31-102) over the active cells:
+ * Bout = Bin + coeff * curl E (coeff = fraction * correction * dt; Bin may
+ * alias Bout) */
+int pic_gr_faraday(pic_ctx* ctx, const pic_gr_metric* m, const void* Bin, void* Bout,
+                   const void* E, double coeff, void* stream);
+/* gr::Ampere_kernel (ampere_gr.hpp:32-101) over i2 in [i2min, i2max + 1):
+ * Dout = Din + coeff * curl H. The axis cells copy dx1 from the neighbouring
+ * row after that row is updated (when Din aliases Dout the reference reads it
+ * unordered). */
+int pic_gr_ampere(pic_ctx* ctx, const pic_gr_metric* m, const void* Din, void* Dout,
+                  const void* H, double coeff, void* stream);
+/* gr::CurrentsAmpere_kernel (ampere_gr.hpp:106-176): D += coeff * J with
+ * the metric factors (coeff = -dt q0 / B0, fieldsolvers.h:216-221) */
+int pic_gr_currents_ampere(pic_ctx* ctx, const pic_gr_metric* m, void* D, const void* J,
+                           double coeff, void* stream);
+/* ComputeAuxE (which = 0) / ComputeAuxH (which = 1) (aux_fields_gr.hpp:27-
+ * 210) over range_with_axis_BCs (fieldsolvers.h:58-81): out's E (or H) from
+ * the D of D and the B of B */
+int pic_gr_aux(pic_ctx* ctx, const pic_gr_metric* m, int32_t which, const void* D, const void* B,
+               void* out, void* stream);
+/* TimeAverageDB (which = 0: b = (b + a) / 2 over the 6 EM components) and
+ * TimeAverageJ (which = 1: a = (b + a) / 2 over the 3 current components),
+ * active cells (aux_fields_gr.hpp:214-280) */
+int pic_gr_average(pic_ctx* ctx, int32_t which, void* a, void* b, void* stream);
+/* AxisBoundaries_kernel and HorizonBoundaries_kernel (fields_bcs.hpp:825-868,
+ * 1188-1240) on one field, per m's axis/horizon flags; set_e / set_b select
+ * the D (E) and B (H) components */
+int pic_gr_field_bcs(pic_ctx* ctx, const pic_gr_metric* m, void* fld, int32_t set_e,
+                     int32_t set_b, int32_t nfilter, void* stream);
+/* the vertical seed field of pgens/wald (InitFields, init_field = vertical)
+ * on every cell, ghosts included; D = 0 */
+int pic_gr_init_vertical(pic_ctx* ctx, const pic_gr_metric* m, void* EB, void* stream);
+/* QKerrSchild::find_dxMin (qkerr_schild.h:112-129): min over cell centres of
+ * 1 / (alpha sqrt(h^11 + h^22) + beta^1); dt = CFL * this. Synchronises. */
+int pic_gr_min_cell_size(pic_ctx* ctx, const pic_gr_metric* m, double* out, void* stream);
+
+/* GR step parameters beyond pic_step_params */
+typedef struct {
+  int32_t niter;      /* pusher iterations (algorithms.gr.pusher_niter, default 10) */
+  int32_t island_i1;  /* particles with i1 below run the pusher in FP64 */
+} pic_gr_params;
+
+/* GRPICEngine::step_forward (src/engines/grpic/grpic.hpp:66-634) on one
+ * domain: fields[0..5] = em, em0, aux, cur, cur0, buff (device pointers);
+ * the step swaps em <-> em0 and cur <-> cur0 in the array as the reference
+ * swaps its views. Step 0 runs the reference's initialisation block.
+ * Filters are not supported (nfilter must be 0); MATCH field boundaries are
+ * not applied (ghost cells at r max keep their values). */
+int pic_grpic_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, int32_t nspecies,
+                   void* fields[6], const pic_step_params* prm, const pic_gr_params* gprm,
+                   int64_t step, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

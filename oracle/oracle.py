@@ -327,3 +327,84 @@ class GROracle(Oracle):
     def gr_field_bcs(self, fld, set_e, set_b, axis_min=1, axis_max=1, horizon=1, nfilter=0):
         self.L.orc_gr_field_bcs(C.byref(self.og), _p(fld), int(set_e), int(set_b), axis_min,
                                 axis_max, horizon, nfilter)
+
+    # GRPICEngine::step_forward (grpic.hpp:66-634), the sequence of the
+    # product's engine: fields = [em, em0, aux, cur, cur0, buff], swapped in
+    # place; axis/horizon boundaries on em and em0 after each update
+    def grpic_step(self, species, fields, prm, niter=10, island_i1=0, step=0, flags=(1, 1, 1)):
+        R = self.g.real
+        t = lambda v: torch.tensor(v, dtype=R)
+        amin, amax, hor = flags
+
+        def bc(set_e, set_b):
+            for f in fields[:2]:
+                self.gr_field_bcs(f, set_e, set_b, amin, amax, hor, prm.nfilter)
+
+        def swap():
+            fields[0], fields[1] = fields[1], fields[0]
+            fields[3], fields[4] = fields[4], fields[3]
+
+        dt = t(prm.dt)
+        dT1 = float(t(1.0) * t(prm.correction) * dt)
+        dTh = float(t(0.5) * t(prm.correction) * dt)
+        jc = float(-dt * t(prm.q0) / t(prm.B0))
+        fs, dep = prm.fieldsolver_enabled, prm.deposit_enabled
+        em, em0, aux = fields[0], fields[1], fields[2]
+        if step == 0:
+            if fs:
+                bc(1, 1)
+                fields[1].copy_(fields[0])
+                em, em0 = fields[0], fields[1]
+                self.gr_aux_e(em, em0, aux, amax)
+                self.gr_aux_h(em, em0, aux, amax)
+                self.gr_faraday(em0, em0, aux, dTh, amin)
+                bc(0, 1)
+                self.gr_ampere(em, em, aux, dTh, amin, amax)
+                bc(1, 0)
+                self.gr_aux_e(em, em0, aux, amax)
+                self.gr_aux_h(em, em0, aux, amax)
+                self.gr_faraday(em, em0, aux, dT1, amin)
+                bc(0, 1)
+                self.gr_ampere(em0, em0, aux, dT1, amin, amax)
+                bc(1, 0)
+                self.gr_aux_h(em0, em0, aux, amax)
+                self.gr_ampere(em, em0, aux, dT1, amin, amax)
+                bc(1, 0)
+                swap()
+            else:
+                fields[1].copy_(fields[0])
+        em, em0 = fields[0], fields[1]
+        if fs:
+            self.gr_average_db(em, em0)
+            self.gr_aux_e(em0, em, aux, amax)
+            self.gr_faraday(em0, em0, aux, dT1, amin)
+            bc(0, 1)
+            self.gr_aux_h(em, em0, aux, amax)
+        for sp in species:
+            if sp.npart > 0 and sp.pusher != 0:
+                self.gr_push(sp, em, em0, float(dt), prm.omegaB0, niter,
+                             island_i1=island_i1)
+        if dep:
+            self.gr_deposit(species, fields[4], float(dt), island_i1=island_i1)
+        if fs:
+            cur, cur0 = fields[3], fields[4]
+            if dep:
+                self.gr_average_j(cur, cur0)
+            self.gr_aux_e(em, em0, aux, amax)
+            self.gr_faraday(em, em0, aux, dT1, amin)
+            bc(0, 1)
+            self.gr_ampere(em0, em0, aux, dT1, amin, amax)
+            if dep:
+                self.gr_currents_ampere(em0, cur, jc, amin, amax)
+            bc(1, 0)
+            self.gr_aux_h(em0, em0, aux, amax)
+            self.gr_ampere(em, em0, aux, dT1, amin, amax)
+            if dep:
+                self.gr_currents_ampere(em0, cur0, jc, amin, amax)
+            swap()
+            bc(1, 0)
+        for sp in species:
+            if prm.clear_interval > 0 and step % prm.clear_interval == 0 and step > 0:
+                self.remove_dead(sp)
+            if prm.sort_interval > 0 and step % prm.sort_interval == 0:
+                self.sort(sp)

@@ -113,3 +113,49 @@ def test_transforms_preserve_the_norm(real):
     # contravariant -> tetrad of u^i equals covariant -> tetrad of u_i
     vt2 = o.transform(1, x, vc)
     assert float(((vt2 - vt).abs()).max()) < tol * 10
+
+
+def test_geodesic_push_conserves_killing_energy_and_angular_momentum():
+    """Without fields the GR pusher integrates geodesics of the stationary,
+    axisymmetric Kerr metric: u_phi (= u_3) is kept to rounding and the Killing
+    energy -u_t = alpha sqrt(1 + h^ij u_i u_j) - beta^1 u_1 to the accuracy of
+    the implicit midpoint scheme."""
+    from entity_gb300.inputs import SpeciesArrays, empty_field
+    g = GridSpec(dim=2, n=(64, 48, 1), order=2, real=torch.float64, periodic=(0, 0, 0),
+                 prtl_bc=((1, 1), (3, 3), (0, 0)))
+    rh = 1.0 + math.sqrt(1.0 - 0.95 ** 2)
+    o = GROracle(g, a=0.95, r_min=0.9 * rh, r_max=20.0)
+    q = o.q
+    # a few particles at rest or with angular momentum, r ~ 8..14, mid-latitudes
+    r = torch.tensor([8.0, 10.0, 12.0, 14.0], dtype=torch.float64)
+    th = torch.tensor([1.2, 1.5708, 1.0, 2.0], dtype=torch.float64)
+    x1 = (torch.log(r - q.r0) - q.chi_min) / q.dchi
+    x2 = (th - q.eta_min) / q.deta
+    n = 4
+    i1, i2 = x1.floor().to(torch.int32), x2.floor().to(torch.int32)
+    d1, d2 = (x1 - i1).to(torch.float32), (x2 - i2).to(torch.float32)
+    u = [torch.zeros(n, dtype=torch.float64), torch.zeros(n, dtype=torch.float64),
+         torch.tensor([0.0, 1.0, 2.0, -1.5], dtype=torch.float64)]
+    z = torch.zeros(n, dtype=torch.int32)
+    zf = torch.zeros(n, dtype=torch.float32)
+    sp = SpeciesArrays([i1, i2, z.clone()], [d1, d2, zf.clone()], [i1.clone(), i2.clone(), z.clone()],
+                       [d1.clone(), d2.clone(), zf.clone()], u, torch.ones(n, dtype=torch.float64),
+                       torch.ones(n, dtype=torch.int16), 1.0, -1.0, 1, n, 1)
+    em = empty_field(g, 6)
+
+    def energy():
+        x = torch.stack([sp.i[0].double() + sp.dx[0].double(),
+                         sp.i[1].double() + sp.dx[1].double()], 1)
+        m = o.metric(x)
+        uu = torch.stack(sp.u, 1)
+        uc = o.transform(0, x, uu)
+        return m["alpha"] * torch.sqrt(1 + (uu * uc).sum(1)) - m["beta1"] * sp.u[0]
+
+    E0 = energy()
+    u3 = sp.u[2].clone()
+    for _ in range(200):
+        o.gr_push(sp, em, em, 0.05, 1.0, 10)
+    assert torch.equal(sp.tag, torch.ones(n, dtype=torch.int16))
+    # the half E pushes round-trip u through the tetrad basis: exact up to rounding
+    assert torch.allclose(sp.u[2], u3, rtol=1e-12, atol=1e-12)
+    assert float(((energy() - E0) / E0).abs().max()) < 1e-3
