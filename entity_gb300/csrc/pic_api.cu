@@ -679,11 +679,28 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
   if (SpeciesBins* b = find_bins(c, sp->index, false)) b->valid = false;
   // scratch layout (8-byte aligned pieces)
   auto          al   = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  const size_t  b_key = al(4 * np), b_rank = al(4 * np), b_dead = al(np), b_drank = al(8 * np);
+  const size_t  b_key = al(4 * np), b_rank = al(4 * np), b_dead = al(np), b_drank = al(4 * np);
   const size_t  b_cnt = al(4 * (nbins + 1)), b_off = al(8 * (nbins + 1)), b_perm = al(4 * np);
   const size_t  b_ptmp = al(4 * np), b_big = al(4 * nbins), b_nbig = al(4);
   const size_t  rb     = (size_t)g.real_bytes;
-  const size_t  b_tmp  = al(np * (rb > 4 ? rb : 4));
+  // the arrays a sort moves, staged side by side
+  pic::GatherSet gs;
+  auto add = [&](void* arr, int esz) {
+    if (!arr) return;
+    gs.arr[gs.n] = arr;
+    gs.esz[gs.n] = esz;
+    ++gs.n;
+  };
+  add(sp->i1, 4), add(sp->i2, 4), add(sp->dx1, 4), add(sp->dx2, 4);
+  if (g.dim == 3) add(sp->i3, 4), add(sp->dx3, 4);
+  if (!skip_prev) {
+    add(sp->i1_prev, 4), add(sp->i2_prev, 4), add(sp->dx1_prev, 4), add(sp->dx2_prev, 4);
+    if (g.dim == 3) add(sp->i3_prev, 4), add(sp->dx3_prev, 4);
+  }
+  add(sp->ux1, (int)rb), add(sp->ux2, (int)rb), add(sp->ux3, (int)rb), add(sp->weight, (int)rb);
+  add(sp->tag, 2);
+  // the arrays are permuted one after the other through one staging buffer
+  const size_t b_tmp = al(np * (rb > 4 ? rb : 4));
   const size_t  need   = b_key + b_rank + b_dead + b_drank + b_cnt + b_off + b_perm + b_ptmp + b_big +
                       b_nbig + b_tmp;
   if (need > c->sort_bytes) {
@@ -717,7 +734,7 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
   base += b_rank;
   a.is_dead = (uint8_t*)base;
   base += b_dead;
-  a.dead_rank = (int64_t*)base;
+  a.dead_rank = (int32_t*)base;
   base += b_drank;
   a.count = (int32_t*)base;
   base += b_cnt;
@@ -731,53 +748,16 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
   base += b_big;
   a.nbig = (int32_t*)base;
   base += b_nbig;
-  void* tmp = base;
-  a.err     = c->d_err;
+  for (int k = 0; k < gs.n; ++k) gs.tmp[k] = base;
+  a.err = c->d_err;
 
-  int64_t     n_dead = 0;
-  cudaError_t e      = pic::sort_build_perm(a, &n_dead, s);
+  cudaError_t e = pic::sort_build_perm(a, s);
   if (e != cudaSuccess) return PIC_ERR_CUDA;
-  const int32_t* perm = a.perm;
-#define PIC_APPLY(T, ptr)                                                    \
-  if ((e = pic::sort_apply<T>((T*)(ptr), tmp, perm, np, s)) != cudaSuccess) \
-    return PIC_ERR_CUDA;
-  PIC_APPLY(int32_t, sp->i1)
-  PIC_APPLY(int32_t, sp->i2)
-  PIC_APPLY(float, sp->dx1)
-  PIC_APPLY(float, sp->dx2)
-  if (g.dim == 3) {
-    PIC_APPLY(int32_t, sp->i3)
-    PIC_APPLY(float, sp->dx3)
-  }
-  if (!skip_prev) {
-    PIC_APPLY(int32_t, sp->i1_prev)
-    PIC_APPLY(int32_t, sp->i2_prev)
-    PIC_APPLY(float, sp->dx1_prev)
-    PIC_APPLY(float, sp->dx2_prev)
-    if (g.dim == 3) {
-      PIC_APPLY(int32_t, sp->i3_prev)
-      PIC_APPLY(float, sp->dx3_prev)
-    }
-  }
-  if (is_f64(c)) {
-    PIC_APPLY(double, sp->ux1)
-    PIC_APPLY(double, sp->ux2)
-    PIC_APPLY(double, sp->ux3)
-    PIC_APPLY(double, sp->weight)
-  } else {
-    PIC_APPLY(float, sp->ux1)
-    PIC_APPLY(float, sp->ux2)
-    PIC_APPLY(float, sp->ux3)
-    PIC_APPLY(float, sp->weight)
-  }
-  PIC_APPLY(int16_t, sp->tag)
-#undef PIC_APPLY
-  int64_t newn = np;
+  if ((e = pic::sort_apply_all(gs, a.perm, np, s)) != cudaSuccess) return PIC_ERR_CUDA;
   if (remove_dead) {
     // particles_sort.cpp:175-191: alive tags on the front, dead on the tail
-    newn = np - n_dead;
-    if ((e = pic::set_tags(sp->tag, 0, newn, PIC_TAG_ALIVE, s)) != cudaSuccess) return PIC_ERR_CUDA;
-    if ((e = pic::set_tags(sp->tag, newn, np, PIC_TAG_DEAD, s)) != cudaSuccess) return PIC_ERR_CUDA;
+    if ((e = pic::set_tags_after_removal(sp->tag, np, a.count + a.dead_bin, s)) != cudaSuccess)
+      return PIC_ERR_CUDA;
   }
   if (tiled) {
     SpeciesBins* b = find_bins(c, sp->index, true);
@@ -790,7 +770,7 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
     }
     if ((e = pic::tile_offsets(a.off, tcells, (int)ntiles, b->tile_start, s)) != cudaSuccess)
       return PIC_ERR_CUDA;
-    const int64_t cap = np - n_dead;  // every binned particle may end up deferred
+    const int64_t cap = np;  // every binned particle may end up deferred
     if (b->ovf_cap < cap || !b->ovf_count) {
       cudaFree(b->ovf);
       b->ovf = nullptr;
@@ -801,14 +781,22 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
         return PIC_ERR_NOMEM;
       b->ovf_cap = cap;
     }
+  }
+  // the one synchronisation of a sort: the dead count and the error word
+  int32_t            n_dead = 0;
+  unsigned long long h_err[4];
+  if (cudaMemcpyAsync(&n_dead, a.count + a.dead_bin, sizeof(int32_t), cudaMemcpyDeviceToHost, s) !=
+        cudaSuccess ||
+      cudaMemcpyAsync(h_err, c->d_err, sizeof(h_err), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return PIC_ERR_CUDA;
+  const int64_t newn = remove_dead ? np - n_dead : np;
+  if (tiled) {
+    SpeciesBins* b = find_bins(c, sp->index, true);
     b->nalive = np - n_dead;
     b->npart  = newn;
     b->valid  = true;
   }
-  unsigned long long h_err[4];
-  if (cudaMemcpyAsync(h_err, c->d_err, sizeof(h_err), cudaMemcpyDeviceToHost, s) != cudaSuccess)
-    return PIC_ERR_CUDA;
-  if (cudaStreamSynchronize(s) != cudaSuccess) return PIC_ERR_CUDA;
   if (npart_out) *npart_out = newn;
   if (remove_dead) sp->npart = newn;
   return h_err[pic::ERR_OUT_OF_GRID] ? PIC_ERR_DEVICE : PIC_OK;

@@ -14,7 +14,10 @@
 //      (possibly huge) dead bin is placed in order directly;
 //   4. every alive bin's index list is sorted ascending (one thread per bin up
 //      to 32 entries, one block per larger bin);
-//   5. every particle array is gathered through the permutation.
+//   5. every particle array is gathered through the permutation and copied
+//      back.
+// Nothing here synchronises with the host; the dead count stays on the
+// device until the caller reads it.
 #include <cuda_runtime.h>
 
 #include "sort.cuh"
@@ -134,6 +137,10 @@ template cudaError_t exclusive_scan<uint8_t, int64_t>(const uint8_t*, int64_t, i
                                                       ScanScratch<int64_t>&, cudaStream_t);
 template cudaError_t exclusive_scan<int64_t, int64_t>(const int64_t*, int64_t, int64_t*,
                                                       ScanScratch<int64_t>&, cudaStream_t);
+template cudaError_t exclusive_scan<uint8_t, int32_t>(const uint8_t*, int64_t, int32_t*,
+                                                      ScanScratch<int32_t>&, cudaStream_t);
+template cudaError_t exclusive_scan<int32_t, int32_t>(const int32_t*, int64_t, int32_t*,
+                                                      ScanScratch<int32_t>&, cudaStream_t);
 
 namespace {
 
@@ -215,21 +222,30 @@ __global__ void k_fix_small(SortArgs a) {
   }
 }
 
-// 4b. large bins: rank by counting, one block per bin (O(m^2 / threads))
+// 4b. large bins: rank by counting (O(m^2 / threads)); blocks stride over
+// the bins the small-bin pass listed, whose number only the device knows
 __global__ void k_fix_big(SortArgs a) {
-  const int     b  = a.big[blockIdx.x];
-  const int64_t lo = a.off[b], hi = a.off[b + 1];
-  const int64_t m  = hi - lo;
-  for (int64_t q = threadIdx.x; q < m; q += blockDim.x) {
-    const int32_t x = a.perm[lo + q];
-    int64_t       r = 0;
-    for (int64_t z = 0; z < m; ++z) r += (a.perm[lo + z] < x);
-    a.perm_tmp[lo + r] = x;
+  const int nbig = *a.nbig;
+  for (int bi = blockIdx.x; bi < nbig; bi += gridDim.x) {
+    const int     b  = a.big[bi];
+    const int64_t lo = a.off[b], hi = a.off[b + 1];
+    const int64_t m  = hi - lo;
+    for (int64_t q = threadIdx.x; q < m; q += blockDim.x) {
+      const int32_t x = a.perm[lo + q];
+      int64_t       r = 0;
+      for (int64_t z = 0; z < m; ++z) r += (a.perm[lo + z] < x);
+      a.perm_tmp[lo + r] = x;
+    }
+    __syncthreads();
+    for (int64_t q = threadIdx.x; q < m; q += blockDim.x) a.perm[lo + q] = a.perm_tmp[lo + q];
+    __syncthreads();
   }
-  __syncthreads();
-  for (int64_t q = threadIdx.x; q < m; q += blockDim.x) a.perm[lo + q] = a.perm_tmp[lo + q];
 }
 
+// 5. one gather per array through perm into its staging buffer, then a
+// copy back. (A single kernel gathering every array at once ran at half the
+// speed on nearly sorted input: its many concurrent scattered streams lose
+// the L2 locality each array's gather has on its own.)
 template <typename T>
 __global__ void k_gather(const T* __restrict__ src, T* __restrict__ dst, const int32_t* perm,
                          int64_t n) {
@@ -239,10 +255,11 @@ __global__ void k_gather(const T* __restrict__ src, T* __restrict__ dst, const i
   }
 }
 
-__global__ void k_set_tags(int16_t* tag, int64_t lo, int64_t hi, int16_t value) {
+__global__ void k_set_tags(int16_t* tag, int64_t np, const int32_t* n_dead) {
+  const int64_t nalive = np - *n_dead;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < hi; i += stride) {
-    tag[i] = value;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np; i += stride) {
+    tag[i] = i < nalive ? (int16_t)PIC_TAG_ALIVE : (int16_t)PIC_TAG_DEAD;
   }
 }
 
@@ -255,7 +272,7 @@ dim3 grid_n(int64_t n) {
 
 }  // namespace
 
-cudaError_t sort_build_perm(SortArgs a, int64_t* n_dead_out, cudaStream_t s) {
+cudaError_t sort_build_perm(SortArgs a, cudaStream_t s) {
   cudaError_t e;
   const int64_t nbins = (int64_t)a.dead_bin + 1;
   e = cudaMemsetAsync(a.count, 0, sizeof(int32_t) * (nbins + 1), s);
@@ -266,19 +283,12 @@ cudaError_t sort_build_perm(SortArgs a, int64_t* n_dead_out, cudaStream_t s) {
   e = exclusive_scan<int32_t, int64_t>(a.count, nbins + 1, a.off, scr, s);
   scr.release(s);
   if (e != cudaSuccess) return e;
-  int32_t n_dead = 0;
-  e = cudaMemcpyAsync(&n_dead, a.count + a.dead_bin, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+  // the rank of every particle among the dead (and, for the alive-only
+  // compaction, the number of dead before it): one scan, whatever the count
+  ScanScratch<int32_t> scr2;
+  e = exclusive_scan<uint8_t, int32_t>(a.is_dead, a.npart, a.dead_rank, scr2, s);
+  scr2.release(s);
   if (e != cudaSuccess) return e;
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-  if (n_dead > 0) {
-    ScanScratch<int64_t> scr2;
-    e = exclusive_scan<uint8_t, int64_t>(a.is_dead, a.npart, a.dead_rank, scr2, s);
-    scr2.release(s);
-    if (e != cudaSuccess) return e;
-  } else if (!a.spatial) {
-    e = cudaMemsetAsync(a.dead_rank, 0, sizeof(int64_t) * a.npart, s);
-    if (e != cudaSuccess) return e;
-  }
   PIC_KL(k_scatter<<<grid_n(a.npart), 256, 0, s>>>(a));
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (a.spatial && a.dead_bin > 0) {
@@ -286,32 +296,35 @@ cudaError_t sort_build_perm(SortArgs a, int64_t* n_dead_out, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     PIC_KL(k_fix_small<<<grid_n(a.dead_bin), 256, 0, s>>>(a));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    int32_t nbig = 0;
-    e = cudaMemcpyAsync(&nbig, a.nbig, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
-    if (e != cudaSuccess) return e;
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-    if (nbig > 0) {
-      PIC_KL(k_fix_big<<<(unsigned)nbig, 256, 0, s>>>(a));
-      if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    }
+    PIC_KL(k_fix_big<<<152 * 2, 256, 0, s>>>(a));
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
-  *n_dead_out = n_dead;
   return cudaSuccess;
 }
 
-template <typename T>
-cudaError_t sort_apply(T* arr, void* tmp, const int32_t* perm, int64_t n, cudaStream_t s) {
-  if (!arr || n <= 0) return cudaSuccess;
-  PIC_KL(k_gather<T><<<grid_n(n), 256, 0, s>>>(arr, (T*)tmp, perm, n));
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  return cudaMemcpyAsync(arr, tmp, sizeof(T) * n, cudaMemcpyDeviceToDevice, s);
+cudaError_t sort_apply_all(const GatherSet& g, const int32_t* perm, int64_t n, cudaStream_t s) {
+  if (n <= 0 || g.n == 0) return cudaSuccess;
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < g.n; ++k) {
+    if (g.esz[k] == 4)
+      PIC_KL(k_gather<int32_t><<<grid_n(n), 256, 0, s>>>((const int32_t*)g.arr[k], (int32_t*)g.tmp[k], perm, n));
+    else if (g.esz[k] == 8)
+      PIC_KL(k_gather<int64_t><<<grid_n(n), 256, 0, s>>>((const int64_t*)g.arr[k], (int64_t*)g.tmp[k], perm, n));
+    else
+      PIC_KL(k_gather<int16_t><<<grid_n(n), 256, 0, s>>>((const int16_t*)g.arr[k], (int16_t*)g.tmp[k], perm, n));
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    e = cudaMemcpyAsync(g.arr[k], g.tmp[k], (size_t)n * g.esz[k], cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
-template cudaError_t sort_apply<int32_t>(int32_t*, void*, const int32_t*, int64_t, cudaStream_t);
-template cudaError_t sort_apply<float>(float*, void*, const int32_t*, int64_t, cudaStream_t);
-template cudaError_t sort_apply<double>(double*, void*, const int32_t*, int64_t, cudaStream_t);
-template cudaError_t sort_apply<int16_t>(int16_t*, void*, const int32_t*, int64_t, cudaStream_t);
+cudaError_t set_tags_after_removal(int16_t* tag, int64_t np, const int32_t* n_dead,
+                                   cudaStream_t s) {
+  if (np <= 0) return cudaSuccess;
+  PIC_KL(k_set_tags<<<grid_n(np), 256, 0, s>>>(tag, np, n_dead));
+  return cudaGetLastError();
+}
 
 namespace {
 __global__ void k_tile_offsets(const int64_t* off, int64_t tile_cells, int ntiles,
@@ -324,12 +337,6 @@ __global__ void k_tile_offsets(const int64_t* off, int64_t tile_cells, int ntile
 cudaError_t tile_offsets(const int64_t* off, int64_t tile_cells, int ntiles, int32_t* tile_start,
                          cudaStream_t s) {
   PIC_KL(k_tile_offsets<<<(ntiles + 256) / 256, 256, 0, s>>>(off, tile_cells, ntiles, tile_start));
-  return cudaGetLastError();
-}
-
-cudaError_t set_tags(int16_t* tag, int64_t lo, int64_t hi, int16_t value, cudaStream_t s) {
-  if (hi <= lo) return cudaSuccess;
-  PIC_KL(k_set_tags<<<grid_n(hi - lo), 256, 0, s>>>(tag, lo, hi, value));
   return cudaGetLastError();
 }
 

@@ -49,7 +49,7 @@ struct SortArgs {
   int32_t*  key;
   int32_t*  rank;
   uint8_t*  is_dead;
-  int64_t*  dead_rank;
+  int32_t*  dead_rank;
   int32_t*  count;  // dead_bin + 2 entries
   int64_t*  off;    // dead_bin + 2 entries
   int32_t*  perm;
@@ -59,14 +59,24 @@ struct SortArgs {
   unsigned long long* err;
 };
 
-// builds perm (new index -> old index); returns the dead count
-cudaError_t sort_build_perm(SortArgs a, int64_t* n_dead_out, cudaStream_t s);
+// builds perm (new index -> old index) without host synchronisation; the
+// dead count is left in count[dead_bin]
+cudaError_t sort_build_perm(SortArgs a, cudaStream_t s);
 
-// arr[i] <- arr[perm[i]] through tmp (tmp holds >= n elements of T)
-template <typename T>
-cudaError_t sort_apply(T* arr, void* tmp, const int32_t* perm, int64_t n, cudaStream_t s);
+// every listed array permuted in place: arr_k[i] <- arr_k[perm[i]], staged
+// through tmp_k (the tmp_k may share one buffer: the arrays go in turn)
+constexpr int kMaxSortArrays = 20;  // 3D with prev arrays needs 17
+struct GatherSet {
+  void* arr[kMaxSortArrays];
+  void* tmp[kMaxSortArrays];
+  int   esz[kMaxSortArrays];  // element bytes: 2, 4 or 8
+  int   n = 0;
+};
+cudaError_t sort_apply_all(const GatherSet& g, const int32_t* perm, int64_t n, cudaStream_t s);
 
-cudaError_t set_tags(int16_t* tag, int64_t lo, int64_t hi, int16_t value, cudaStream_t s);
+// tags of [0, np - *n_dead) alive and of the rest dead (RemoveDead)
+cudaError_t set_tags_after_removal(int16_t* tag, int64_t np, const int32_t* n_dead,
+                                   cudaStream_t s);
 
 // tile_start[t] = off[t * tile_cells] for t in [0, ntiles]
 cudaError_t tile_offsets(const int64_t* off, int64_t tile_cells, int ntiles, int32_t* tile_start,

@@ -197,8 +197,8 @@ def test_grpic_step_matches_oracle(real):
     torch.cuda.synchronize()
     assert ctx.device_errors() == [0, 0, 0, 0]
     # FP32: the current sums' order differs (atomics) and the step feeds J
-    # back into D; five steps keep the difference below 5e-4 of each scale
-    tol = 5e-4 if real == torch.float32 else 1e-9
+    # back into D; five steps keep the difference below 2e-3 of each scale
+    tol = 2e-3 if real == torch.float32 else 1e-9
     for k, name in ((0, "em"), (1, "em0"), (3, "cur"), (4, "cur0")):
         a, b = cpu_fields[k].double(), fields[k].cpu().double()
         for c in range(a.shape[0]):
