@@ -43,12 +43,12 @@ WORKLOADS = {
                         "4 filter passes, FP32", dim=3, n=(256, 256, 256), order=2, ppc=8,
                    temp=0.09, drift=0.0, nfilter=4, cfl=0.45, skindepth0=10.0, larmor0=10.0,
                    ppc0=16.0, field="turbulent", modes=8, dB=1.0, sample_n=(64, 64, 64),
-                   precision_n=(64, 64, 64), precision_steps=200),
+                   precision_n=(64, 64, 64), precision_steps=200, sort_interval=8),
     "pair2d": dict(name="2D SR pair plasma 512^2, e-/e+ 16 ppc each, drift +-0.3c, order 1, FP32",
                    dim=2, n=(512, 512, 1), order=1, ppc=16, temp=0.01, drift=0.3, nfilter=0,
                    cfl=0.45, skindepth0=10.0, larmor0=10.0, ppc0=16.0, field="none", modes=0,
                    dB=0.0, sample_n=(128, 128, 1), precision_n=(512, 512, 1),
-                   precision_steps=100),
+                   precision_steps=100, sort_interval=16),
     # magnetized uniform plasma: sigma = (skin depth / Larmor radius)^2 = 10,
     # Maxwell-Juttner theta = 1, uniform B0 along x3
     # two cold beams at +-0.2c (16 ppc each) with weights 1 + 1e-3 cos(k x),
@@ -60,17 +60,19 @@ WORKLOADS = {
     # Kerr (a = 0.95) quasi-spherical Kerr-Schild grid, r log-spaced in
     # [0.9 r_h, 50 r_g], theta in [0, pi], vertical seed field, e-/e+ at rest
     # 4 per cell in r < 6 r_g; FP32 with the pusher in FP64 within 3 cells of
-    # the horizon
+    # the horizon (either side)
     "wald2d": dict(name="2D GR Wald problem 1024(r) x 512(theta), a 0.95, vertical field, "
                         "e-/e+ 4 ppc in r < 6, order 2, FP32 with FP64 near the horizon",
                    dim=2, n=(1024, 512, 1), order=2, a=0.95, r_max=50.0, ppc=4, r_inject=6.0,
                    cfl=0.5, skindepth0=0.05, larmor0=0.0025, ppc0=2.0, niter=10,
-                   sort_interval=0, clear_interval=100),
+                   sort_interval=0, clear_interval=100, precision_n=(512, 256),
+                   precision_steps=200),
     "sweep3d": dict(name="3D SR magnetized uniform plasma 192^3, e-/e+ 32 ppc each, sigma 10, "
                          "theta 1, order 3, FP32 vs FP64", dim=3, n=(192, 192, 192), order=3,
                     ppc=32, temp=1.0, drift=0.0, nfilter=0, cfl=0.45, skindepth0=10.0,
                     larmor0=10.0 / math.sqrt(10.0), ppc0=64.0, field="uniform", modes=0, dB=0.0,
-                    sample_n=(24, 24, 24), precision_n=(192, 192, 192), precision_steps=1000),
+                    sample_n=(24, 24, 24), precision_n=(192, 192, 192), precision_steps=1000,
+                    sort_interval=4),
 }
 
 # algorithmic bytes of the fused push+deposit, FP32: per particle read
@@ -91,6 +93,19 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def reduce_over_ranks(t_ms, units, world, device):
+    """Replicas: the job's time is the slowest rank's, its work the sum of
+    every rank's units. Returns (max t_ms, total units)."""
+    if world <= 1:
+        return t_ms, units
+    import torch.distributed as dist
+    tt = torch.tensor([float(t_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    nn = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(nn)
+    return float(tt), float(nn)
 
 
 def make_setup(w, device, n=None):
@@ -331,16 +346,7 @@ def run_ours(args, w):
     t_ms = ev0.elapsed_time(ev1)
     phases = ctx.read_timers()
     ctx.timers(False)
-    t_max = t_ms
-    tot_part = npart
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt)
-        nn = torch.tensor([float(npart)], device="cuda")
-        dist.all_reduce(nn)
-        tot_part = float(nn)
+    t_max, tot_part = reduce_over_ranks(t_ms, npart, world, "cuda")
     value = tot_part * args.steps / (t_max / 1e3)
 
     # dominant kernel: the fused push+deposit (both species), timed by events
@@ -379,7 +385,7 @@ def run_ours(args, w):
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         barrier()
-        te = max(a0.elapsed_time(a1) / 1e3, 1e-9)
+        te, _ = reduce_over_ranks(max(a0.elapsed_time(a1) / 1e3, 1e-9), 0, world, "cuda")
         e2e = {"value": tot_part * k2 / te, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes, "steps": k2, "wall_s": wall}
 
@@ -448,10 +454,18 @@ def run_adjoint(args, w):
         sp, U, W, EB0 = A.build(g, kappa, k, beta, amp, w["ppc"], ctx)
         out = {"particles": sum(s.npart for s in sp)}
         if timed:
-            # warm-up, then the plain forward and the full gradient, both timed
+            # warm-up; the first gradient call allocates the checkpoint slots
+            # (timed apart as gradient_first_ms); then the plain forward and
+            # the steady-state gradient, both timed
             A.forward_energy(ctx, g, prm, sp, U, W, EB0, min(nsteps, 5))
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            L0 = A.energy(ctx, g, prm, sp, U, W, EB0, nsteps, every)
+            torch.autograd.grad(L0, [beta, amp], retain_graph=True)
+            e1.record()
+            torch.cuda.synchronize()
+            out["gradient_first_ms"] = e0.elapsed_time(e1)
             l0 = lib.pic_kernel_launches()
             e0.record()
             out["L_forward"] = A.forward_energy(ctx, g, prm, sp, U, W, EB0, nsteps)
@@ -512,6 +526,7 @@ def run_adjoint(args, w):
                    "checkpoint_every": every, "sort_interval": 0, "parallelism": "replicas x1"},
         "adjoint": {"ratio_gradient_to_forward": r32["gradient_ms"] / r32["forward_ms"],
                     "forward_ms": r32["forward_ms"], "gradient_ms": r32["gradient_ms"],
+                    "gradient_first_ms": r32["gradient_first_ms"],
                     "L": r32["L"], "L_forward": r32["L_forward"], "checks": checks},
         "gpu_launches": r32["forward_launches"],
         "clocks": clocks,
@@ -537,7 +552,7 @@ def run_wald(args, w):
     island = horizon_island(g, spec)
     npart0 = sum(s.npart for s in species)
     for k in range(args.warmup):
-        ctx.grpic_step(species, fields, prm, niter=w["niter"], island_i1=island, step=k)
+        ctx.grpic_step(species, fields, prm, niter=w["niter"], island=island, step=k)
     torch.cuda.synchronize()
     ctx.timers(True)
     sampler = ClockSampler(local)
@@ -549,7 +564,7 @@ def run_wald(args, w):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         steps_particles += sum(s.npart for s in species)
         a.record()
-        ctx.grpic_step(species, fields, prm, niter=w["niter"], island_i1=island,
+        ctx.grpic_step(species, fields, prm, niter=w["niter"], island=island,
                        step=args.warmup + k)
         b.record()
         ev.append((a, b))
@@ -566,14 +581,59 @@ def run_wald(args, w):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": w["name"], "cells": n[0] * n[1], "particles_initial": npart0,
                    "particles_final": sum(s.npart for s in species), "dt": prm.dt,
-                   "fp64_island_i1": island, "parallelism": "replicas x1"},
+                   "fp64_island_cells": list(island), "parallelism": "replicas x1"},
         "ns_per_particle_step": 1e9 / value,
         "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in phases.items()},
         "device_errors": errs,
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    psteps = w["precision_steps"] if args.precision_steps is None else args.precision_steps
+    if psteps > 0:
+        line["precision"] = wald_precision(w, w["precision_n"], psteps)
     print(json.dumps(line), flush=True)
+
+
+def wald_precision(w, n, steps):
+    """The FP32 step (with and without the FP64 island) against the FP64
+    step from the same seeded Wald set-up: relative L2 error of D and B,
+    and the particle state error of particles alive in all three runs
+    (dead particles are not removed, so indices stay aligned)."""
+    from entity_gb300.gr import gr_step_params, horizon_island, wald_setup
+    runs = {}
+    for tag, real, isl in (("f64", torch.float64, True), ("f32_island", torch.float32, True),
+                           ("f32_no_island", torch.float32, False)):
+        g, spec, ctx, fields, species = wald_setup(n=n, a=w["a"], r_max=w["r_max"],
+                                                   order=w["order"], ppc=w["ppc"],
+                                                   r_inject=w["r_inject"], real=real)
+        prm = gr_step_params(ctx, cfl=w["cfl"], ppc0=w["ppc0"], skindepth0=w["skindepth0"],
+                             larmor0=w["larmor0"], sort_interval=0, clear_interval=0)
+        island = horizon_island(g, spec) if isl else (0, 0)
+        for k in range(steps):
+            ctx.grpic_step(species, fields, prm, niter=w["niter"], island=island, step=k)
+        torch.cuda.synchronize()
+        ng = g.ng
+        em = fields[0][:, 0, ng:ng + n[1], ng:ng + n[0]].double()
+        X = [torch.stack([s.i[d].double() + s.dx[d].double() for d in range(2)]) for s in species]
+        U = [torch.stack([u.double() for u in s.u]) for s in species]
+        alive = [s.tag == 1 for s in species]
+        runs[tag] = (em, X, U, alive, island)
+    ref = runs["f64"]
+    out = {"steps": steps, "cells": list(n), "fp64_island_cells": list(runs["f32_island"][4])}
+    for tag in ("f32_island", "f32_no_island"):
+        em, X, U, alive, _ = runs[tag]
+        both = [a & b for a, b in zip(alive, ref[3])]
+        dx = max(float((x - xr)[:, m].abs().max()) if m.any() else 0.0
+                 for x, xr, m in zip(X, ref[1], both))
+        du = max(float(((u - ur)[:, m]).norm() / (ur[:, m].norm() + 1e-300)) if m.any() else 0.0
+                 for u, ur, m in zip(U, ref[2], both))
+        out[tag] = {
+            "D_rel_l2": float((em[:3] - ref[0][:3]).norm() / ref[0][:3].norm()),
+            "B_rel_l2": float((em[3:] - ref[0][3:]).norm() / ref[0][3:].norm()),
+            "x_max_abs_cells": dx, "u_rel_l2": du,
+            "alive_mismatch": int(sum(int((a != b).sum()) for a, b in zip(alive, ref[3]))),
+        }
+    return out
 
 
 def run_sweep(args, w):
@@ -635,7 +695,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="turb3d", choices=sorted(WORKLOADS))
-    ap.add_argument("--sort-interval", type=int, default=4)
+    ap.add_argument("--sort-interval", type=int, default=None,
+                    help="steps between tile-major sorts (default: the workload's)")
     ap.add_argument("--reference-sort-key", action="store_true",
                     help="sort by the reference's i1-major cell key (untiled push/deposit)")
     ap.add_argument("--cells", type=int, nargs="+", default=None,
@@ -653,6 +714,8 @@ def main():
                     help="forward steps of the adjoint workload (default 400)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
+    if args.sort_interval is None:
+        args.sort_interval = w.get("sort_interval", 4)
     if args.cells is not None:
         c = list(args.cells) + [1] * (3 - len(args.cells))
         args.cells = tuple(c)

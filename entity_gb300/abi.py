@@ -83,7 +83,7 @@ class PicGRMetric(C.Structure):
 
 
 class PicGRParams(C.Structure):
-    _fields_ = [("niter", C.c_int32), ("island_i1", C.c_int32)]
+    _fields_ = [("niter", C.c_int32), ("island_lo", C.c_int32), ("island_hi", C.c_int32)]
 
 
 class PicStepParams(C.Structure):
@@ -147,9 +147,9 @@ SIGNATURES = {
                                      C.c_int64, C.c_int64, _VP, C.POINTER(C.c_double), _VP]),
     "pic_gr_metric_eval": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, C.c_int64, _VP, _VP]),
     "pic_gr_push": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.POINTER(PicSpecies), _VP, _VP,
-                              C.c_double, C.c_double, C.c_int32, C.c_int32, _VP]),
+                              C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_int32, _VP]),
     "pic_gr_deposit": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.POINTER(PicSpecies), C.c_int32,
-                                 _VP, C.c_double, C.c_int32, C.c_uint32, _VP]),
+                                 _VP, C.c_double, C.c_int32, C.c_int32, C.c_uint32, _VP]),
     "pic_gr_faraday": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP, _VP, C.c_double, _VP]),
     "pic_gr_ampere": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP, _VP, C.c_double, _VP]),
     "pic_gr_currents_ampere": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP, C.c_double,

@@ -45,6 +45,16 @@ struct pic_ctx {
   std::vector<cudaEvent_t>                        event_pool;
   // checkpoint and snapshot storage of pic_srpic_gradient (grown on demand)
   pic::AdjointScratch*                            adjoint = nullptr;
+  // indices of the GR pusher's FP64-island particles followed by their
+  // membership bitmask (grown on demand), and two counters: the list length
+  // and the island kernel's work cursor
+  int32_t*                                        gr_island     = nullptr;
+  int64_t                                         gr_island_cap = 0;
+  unsigned*                                       gr_island_cnt = nullptr;
+  // second stream of the island kernel, forked from and joined to the
+  // caller's stream by the two events
+  cudaStream_t                                    gr_side = nullptr;
+  cudaEvent_t                                     gr_fork = nullptr, gr_join = nullptr;
 };
 
 namespace pic_internal {

@@ -4,8 +4,9 @@
 //     shape-order interpolation of D (em) and B (em0), half E push, implicit
 //     geodesic momentum push, half E push, implicit coordinate push, the
 //     absorbing-r / axis-theta particle boundaries. Particles within a few
-//     cells of the horizon (i1 < island_i1) run the metric and both implicit
-//     iterations in double; the rest in the field precision;
+//     cells of the horizon (the FP64 island, island_lo <= i1 < island_hi)
+//     run the metric and both implicit iterations in double, in a kernel of
+//     their own that overlaps the single-precision bulk;
 //   - current deposit (DepositCurrents_kernel, GR branch, shape order 1,
 //     currents_deposit.hpp:138-159) with the metric out-of-plane velocity;
 //   - field kernels (faraday_gr.hpp, ampere_gr.hpp, aux_fields_gr.hpp) and
@@ -34,8 +35,11 @@ struct GRPushArgs {
   int             n1, n2, ng;
   int             absorb_min, absorb_max, axis_min, axis_max;
   real            dt, ndth;
-  int             niter, island, massive;
+  int             niter, island_lo, island_hi, massive;
   unsigned long long* err;
+  int32_t*        list;        // island indices, or null: no island split
+  unsigned*       list_count;  // [0] list length, [1] island work cursor
+  unsigned*       mask;        // bit p: particle p is on the list
 };
 
 // D from em (components 0..2) and B from em0 (3..5) at the particle
@@ -170,76 +174,138 @@ __device__ __forceinline__ void gr_push_one(const QKS<M>& m, bool massive, M ndt
   uo[0] = vu[0], uo[1] = vu[1], uo[2] = vu[2];
 }
 
+// one particle: interpolation, the push in the island's or the field
+// precision, the particle boundaries (gr.hpp:664-865)
+template <int O, bool ISLAND, typename real>
+__device__ __forceinline__ void gr_push_particle(const GRPushArgs<real>& a, int64_t p) {
+  real* ux[3] = { (real*)a.sp.ux1, (real*)a.sp.ux2, (real*)a.sp.ux3 };
+  const int   i1 = a.sp.i1[p], i2 = a.sp.i2[p];
+  const float d1 = a.sp.dx1[p], d2 = a.sp.dx2[p];
+  if (i1 < 0 || i1 >= a.n1 || i2 < 0 || i2 >= a.n2) {
+    atomicAdd(a.err + ERR_OUT_OF_GRID, 1ull);
+    return;
+  }
+  a.sp.i1p[p]  = i1;
+  a.sp.i2p[p]  = i2;
+  a.sp.dx1p[p] = d1;
+  a.sp.dx2p[p] = d2;
+  real Dc[3] = { 0, 0, 0 }, Bc[3] = { 0, 0, 0 };
+  if (a.massive) {
+    const int  ic[2] = { i1 + a.ng, i2 + a.ng };
+    const real dc[2] = { (real)d1, (real)d2 };
+    interp_db<O, real>(a.em, a.em0, ic, dc, Dc, Bc);
+  }
+  // i_di_to_Xi in real_t (gr.hpp:45)
+  const real X0 = (real)i1 + (real)d1, X1 = (real)i2 + (real)d2;
+  real       xo[2], uo[3];
+  if (ISLAND) {
+    const double xp[2] = { (double)X0, (double)X1 };
+    const double Dd[3] = { (double)Dc[0], (double)Dc[1], (double)Dc[2] };
+    const double Bd[3] = { (double)Bc[0], (double)Bc[1], (double)Bc[2] };
+    const double ud[3] = { (double)ux[0][p], (double)ux[1][p], (double)ux[2][p] };
+    double       xd[2], uo_d[3];
+    gr_push_one<double>(a.m, a.massive, (double)a.ndth, (double)a.dt, a.niter, xp, Dd, Bd, ud, xd,
+                        uo_d);
+    xo[0] = (real)xd[0], xo[1] = (real)xd[1];
+    uo[0] = (real)uo_d[0], uo[1] = (real)uo_d[1], uo[2] = (real)uo_d[2];
+  } else {
+    const QKS<real> m     = a.m.template as<real>();
+    const real      xp[2] = { X0, X1 };
+    const real      ur[3] = { ux[0][p], ux[1][p], ux[2][p] };
+    gr_push_one<real>(m, a.massive, a.ndth, a.dt, a.niter, xp, Dc, Bc, ur, xo, uo);
+  }
+  // from_Xi_to_i_di (gr.hpp:34-43)
+  int     j1 = (int)(xo[0] + (real)1) - 1, j2 = (int)(xo[1] + (real)1) - 1;
+  float   e1 = (float)xo[0] - (float)j1, e2 = (float)xo[1] - (float)j2;
+  int16_t ntag = PIC_TAG_ALIVE;
+  // boundaryConditions (gr.hpp:818-865)
+  if ((j1 < 0 && a.absorb_min) || (j1 >= a.n1 && a.absorb_max)) ntag = PIC_TAG_DEAD;
+  if (j2 < 0) {
+    if (a.axis_min) {
+      j2    = 0;
+      e2    = 1.0f - e2;
+      uo[1] = -uo[1];
+    }
+  } else if (j2 >= a.n2) {
+    if (a.axis_max) {
+      j2    = a.n2 - 1;
+      e2    = 1.0f - e2;
+      uo[1] = -uo[1];
+    }
+  }
+  a.sp.i1[p]  = j1;
+  a.sp.i2[p]  = j2;
+  a.sp.dx1[p] = e1;
+  a.sp.dx2[p] = e2;
+  ux[0][p] = uo[0], ux[1][p] = uo[1], ux[2][p] = uo[2];
+  if (ntag != PIC_TAG_ALIVE) a.sp.tag[p] = ntag;
+}
+
+template <typename real>
+__device__ __forceinline__ bool in_island(const GRPushArgs<real>& a, int i1) {
+  return i1 >= a.island_lo && i1 < a.island_hi;
+}
+
+// Live particles of the FP64 island appended to a.list (warp-aggregated
+// atomics), ahead of the two push kernels, and marked in a.mask: the two
+// kernels run at once and the island kernel moves its particles, so the
+// bulk decides membership from the mask, never from i1. A warp covers 32
+// consecutive particles starting at a multiple of 32 (block size and grid
+// stride are multiples of 32), and its ballot is their mask word.
+template <typename real>
+__global__ void __launch_bounds__(256) k_gr_island_list(GRPushArgs<real> a) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int     lane   = threadIdx.x & 31;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.sp.npart; p += stride) {
+    const bool     isl = a.sp.tag[p] == PIC_TAG_ALIVE && in_island(a, a.sp.i1[p]);
+    const unsigned act = __activemask();
+    const unsigned bal = __ballot_sync(act, isl);
+    if (lane == __ffs(act) - 1) a.mask[p >> 5] = bal;
+    if (bal) {
+      const int leader = __ffs(bal) - 1;
+      unsigned  base   = 0;
+      if (lane == leader) base = atomicAdd(a.list_count, (unsigned)__popc(bal));
+      base = __shfl_sync(act, base, leader);
+      if (isl) a.list[base + __popc(bal & ((1u << lane) - 1u))] = (int32_t)p;
+    }
+  }
+}
+
+// The bulk: every live particle outside the island, in the field
+// precision. With a.list null (FP64 fields, or no island) every particle is
+// pushed here.
 template <int O, typename real>
 __global__ void __launch_bounds__(256) k_gr_push(GRPushArgs<real> a) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  real*         ux[3]  = { (real*)a.sp.ux1, (real*)a.sp.ux2, (real*)a.sp.ux3 };
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.sp.npart; p += stride) {
     const int16_t tag = a.sp.tag[p];
     if (tag != PIC_TAG_ALIVE) {
       if (tag != PIC_TAG_DEAD) atomicAdd(a.err + ERR_BAD_TAG, 1ull);
       continue;
     }
-    const int   i1 = a.sp.i1[p], i2 = a.sp.i2[p];
-    const float d1 = a.sp.dx1[p], d2 = a.sp.dx2[p];
-    if (i1 < 0 || i1 >= a.n1 || i2 < 0 || i2 >= a.n2) {
-      atomicAdd(a.err + ERR_OUT_OF_GRID, 1ull);
-      continue;
-    }
-    a.sp.i1p[p]  = i1;
-    a.sp.i2p[p]  = i2;
-    a.sp.dx1p[p] = d1;
-    a.sp.dx2p[p] = d2;
-    real Dc[3] = { 0, 0, 0 }, Bc[3] = { 0, 0, 0 };
-    if (a.massive) {
-      const int  ic[2] = { i1 + a.ng, i2 + a.ng };
-      const real dc[2] = { (real)d1, (real)d2 };
-      interp_db<O, real>(a.em, a.em0, ic, dc, Dc, Bc);
-    }
-    // i_di_to_Xi in real_t (gr.hpp:45)
-    const real X0 = (real)i1 + (real)d1, X1 = (real)i2 + (real)d2;
-    real       xo[2], uo[3];
-    if (i1 < a.island) {
-      const double xp[2] = { (double)X0, (double)X1 };
-      const double Dd[3] = { (double)Dc[0], (double)Dc[1], (double)Dc[2] };
-      const double Bd[3] = { (double)Bc[0], (double)Bc[1], (double)Bc[2] };
-      const double ud[3] = { (double)ux[0][p], (double)ux[1][p], (double)ux[2][p] };
-      double       xd[2], uo_d[3];
-      gr_push_one<double>(a.m, a.massive, (double)a.ndth, (double)a.dt, a.niter, xp, Dd, Bd, ud, xd,
-                          uo_d);
-      xo[0] = (real)xd[0], xo[1] = (real)xd[1];
-      uo[0] = (real)uo_d[0], uo[1] = (real)uo_d[1], uo[2] = (real)uo_d[2];
-    } else {
-      const QKS<real> m     = a.m.template as<real>();
-      const real      xp[2] = { X0, X1 };
-      const real      ur[3] = { ux[0][p], ux[1][p], ux[2][p] };
-      gr_push_one<real>(m, a.massive, a.ndth, a.dt, a.niter, xp, Dc, Bc, ur, xo, uo);
-    }
-    // from_Xi_to_i_di (gr.hpp:34-43)
-    int   j1 = (int)(xo[0] + (real)1) - 1, j2 = (int)(xo[1] + (real)1) - 1;
-    float e1 = (float)xo[0] - (float)j1, e2 = (float)xo[1] - (float)j2;
-    int16_t ntag = PIC_TAG_ALIVE;
-    // boundaryConditions (gr.hpp:818-865)
-    if ((j1 < 0 && a.absorb_min) || (j1 >= a.n1 && a.absorb_max)) ntag = PIC_TAG_DEAD;
-    if (j2 < 0) {
-      if (a.axis_min) {
-        j2    = 0;
-        e2    = 1.0f - e2;
-        uo[1] = -uo[1];
-      }
-    } else if (j2 >= a.n2) {
-      if (a.axis_max) {
-        j2    = a.n2 - 1;
-        e2    = 1.0f - e2;
-        uo[1] = -uo[1];
-      }
-    }
-    a.sp.i1[p]  = j1;
-    a.sp.i2[p]  = j2;
-    a.sp.dx1[p] = e1;
-    a.sp.dx2[p] = e2;
-    ux[0][p] = uo[0], ux[1][p] = uo[1], ux[2][p] = uo[2];
-    if (ntag != PIC_TAG_ALIVE) a.sp.tag[p] = ntag;
+    if (a.list != nullptr && ((a.mask[p >> 5] >> (p & 31)) & 1u)) continue;
+    gr_push_particle<O, false, real>(a, p);
+  }
+}
+
+// The island list, in chunks of 32 entries handed out to warps by a device
+// cursor: each warp takes chunks until the list (read once) is exhausted.
+// Island particles are cell-sorted into a few contiguous blocks of the
+// particle arrays; pushed in place, their FP64 work (GB300 runs FP64 at
+// 1/64 of the FP32 rate) would sit on the few SMs holding those blocks. This
+// kernel runs on a second stream beside the bulk, so the FP64 and FP32 pipes
+// work at once.
+template <int O, typename real>
+__global__ void __launch_bounds__(128, 3) k_gr_push_island(GRPushArgs<real> a) {
+  const int      lane = threadIdx.x & 31;
+  const unsigned n    = a.list_count[0];
+  for (;;) {
+    unsigned chunk = 0;
+    if (lane == 0) chunk = atomicAdd(a.list_count + 1, 1u);
+    chunk = __shfl_sync(0xffffffffu, chunk, 0);
+    if ((uint64_t)chunk * 32u >= n) break;
+    const unsigned j = chunk * 32u + (unsigned)lane;
+    if (j < n) gr_push_particle<O, true, real>(a, a.list[j]);
   }
 }
 
@@ -251,7 +317,7 @@ struct GRDepArgs {
   SpeciesPtrs     sp;
   FieldView<real> J;
   QKS<double>     m;
-  int             ng, island;
+  int             ng, island_lo, island_hi;
   int             ext[3];
   real            inv_dt, charge;
   unsigned long long* err;
@@ -281,7 +347,7 @@ __global__ void __launch_bounds__(256) k_gr_deposit(GRDepArgs<real> a) {
     q.dxp[0] = a.sp.dx1p[p], q.dxp[1] = a.sp.dx2p[p], q.dxp[2] = 0.0f;
     const real X0 = (real)q.i[0] + (real)q.dx[0], X1 = (real)q.i[1] + (real)q.dx[1];
     real       vp[3] = { 0, 0, 0 };
-    if (q.i[0] < a.island) {
+    if (q.i[0] >= a.island_lo && q.i[0] < a.island_hi) {
       const double ud[3] = { (double)ux[0][p], (double)ux[1][p], (double)ux[2][p] };
       vp[2]              = (real)gr_vz<double>(a.m, (double)X0, (double)X1, ud);
     } else {
@@ -678,10 +744,34 @@ pic::Range2 active(const pic_ctx* c) {
   return pic::Range2{ ng, c->grid.n[0] + ng, ng, c->grid.n[1] + ng };
 }
 
+// the island list's buffers, the side stream and its events, made on first use
+int island_resources(pic_ctx* c, int64_t npart) {
+  if (!c->gr_island_cnt &&
+      cudaMalloc((void**)&c->gr_island_cnt, 2 * sizeof(unsigned)) != cudaSuccess)
+    return PIC_ERR_NOMEM;
+  if (c->gr_island_cap < npart) {
+    cudaFree(c->gr_island);
+    c->gr_island     = nullptr;
+    c->gr_island_cap = 0;
+    // the list (npart entries) followed by the mask (one bit per particle)
+    const int64_t words = npart + (npart + 31) / 32;
+    if (cudaMalloc((void**)&c->gr_island, sizeof(int32_t) * words) != cudaSuccess)
+      return PIC_ERR_NOMEM;
+    c->gr_island_cap = npart;
+  }
+  if (!c->gr_side && cudaStreamCreateWithFlags(&c->gr_side, cudaStreamNonBlocking) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  if (!c->gr_fork && cudaEventCreateWithFlags(&c->gr_fork, cudaEventDisableTiming) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  if (!c->gr_join && cudaEventCreateWithFlags(&c->gr_join, cudaEventDisableTiming) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  return PIC_OK;
+}
+
 template <typename real>
 int gr_push(pic_ctx* c, const pic_gr_metric* g, const pic_species* sp, const void* em,
-            const void* em0, double dt, double omegaB0, int32_t niter, int32_t island,
-            cudaStream_t s) {
+            const void* em0, double dt, double omegaB0, int32_t niter, int32_t island_lo,
+            int32_t island_hi, cudaStream_t s) {
   pic::GRPushArgs<real> a;
   a.sp  = sptrs(sp);
   a.em  = em_view<real>(c, em);
@@ -696,28 +786,68 @@ int gr_push(pic_ctx* c, const pic_gr_metric* g, const pic_species* sp, const voi
   const float qm = sp->pusher == PIC_PUSHER_PHOTON ? 0.0f : sp->charge / sp->mass;
   a.ndth       = (real)0.5 * (real)qm * (real)omegaB0 * (real)dt;
   a.niter      = niter;
-  a.island     = sizeof(real) == 8 ? (1 << 30) : island;
+  a.island_lo  = island_lo;
+  a.island_hi  = island_hi;
   a.massive    = sp->pusher != PIC_PUSHER_PHOTON;
   a.err        = c->d_err;
-  const unsigned b = blocks_for(sp->npart);
-  switch (c->grid.order) {
-    case 1: PIC_KL(pic::k_gr_push<1, real><<<b, 256, 0, s>>>(a)); break;
-    case 2: PIC_KL(pic::k_gr_push<2, real><<<b, 256, 0, s>>>(a)); break;
-    case 3: PIC_KL(pic::k_gr_push<3, real><<<b, 256, 0, s>>>(a)); break;
-    default: return PIC_ERR_UNSUPPORTED;
+  a.list       = nullptr;
+  a.list_count = nullptr;
+  a.mask       = nullptr;
+  if (c->grid.order < 1 || c->grid.order > 3) return PIC_ERR_UNSUPPORTED;
+  const unsigned b     = blocks_for(sp->npart);
+  auto           bulk  = [&]() {
+    switch (c->grid.order) {
+      case 1: PIC_KL(pic::k_gr_push<1, real><<<b, 256, 0, s>>>(a)); break;
+      case 2: PIC_KL(pic::k_gr_push<2, real><<<b, 256, 0, s>>>(a)); break;
+      default: PIC_KL(pic::k_gr_push<3, real><<<b, 256, 0, s>>>(a)); break;
+    }
+  };
+  // double fields run everything in double: no split
+  if (sizeof(real) == 8 || island_hi <= island_lo) {
+    bulk();
+    return cuda_status(cudaGetLastError());
   }
+  // the island list holds 32-bit particle indices
+  if (sp->npart > (int64_t)INT32_MAX) return PIC_ERR_UNSUPPORTED;
+  int st = island_resources(c, sp->npart);
+  if (st != PIC_OK) return st;
+  a.list       = c->gr_island;
+  a.list_count = c->gr_island_cnt;
+  a.mask       = reinterpret_cast<unsigned*>(c->gr_island + c->gr_island_cap);
+  if (cudaMemsetAsync(c->gr_island_cnt, 0, 2 * sizeof(unsigned), s) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  PIC_KL(pic::k_gr_island_list<real><<<b, 256, 0, s>>>(a));
+  // fork: the island on the side stream beside the bulk on s; join
+  if (cudaEventRecord(c->gr_fork, s) != cudaSuccess ||
+      cudaStreamWaitEvent(c->gr_side, c->gr_fork, 0) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  if constexpr (sizeof(real) == 4) {
+    // three 128-thread blocks per SM fit at up to 170 registers per thread
+    const unsigned bi = 152 * 3;
+    cudaStream_t   s2 = c->gr_side;
+    switch (c->grid.order) {
+      case 1: PIC_KL(pic::k_gr_push_island<1, real><<<bi, 128, 0, s2>>>(a)); break;
+      case 2: PIC_KL(pic::k_gr_push_island<2, real><<<bi, 128, 0, s2>>>(a)); break;
+      default: PIC_KL(pic::k_gr_push_island<3, real><<<bi, 128, 0, s2>>>(a)); break;
+    }
+  }
+  if (cudaEventRecord(c->gr_join, c->gr_side) != cudaSuccess) return PIC_ERR_CUDA;
+  bulk();
+  if (cudaStreamWaitEvent(s, c->gr_join, 0) != cudaSuccess) return PIC_ERR_CUDA;
   return cuda_status(cudaGetLastError());
 }
 
 template <typename real>
 int gr_deposit(pic_ctx* c, const pic_gr_metric* g, const pic_species* sp, void* J, double dt,
-               int32_t island, cudaStream_t s) {
+               int32_t island_lo, int32_t island_hi, cudaStream_t s) {
   pic::GRDepArgs<real> a;
   a.sp = sptrs(sp);
   a.J  = cur_view<real>(c, J);
   a.m  = make_qks<real>(c, g);
   a.ng = c->grid.ng;
-  a.island = sizeof(real) == 8 ? (1 << 30) : island;
+  // double fields: the field precision is already double
+  a.island_lo = sizeof(real) == 8 ? 1 : island_lo;
+  a.island_hi = sizeof(real) == 8 ? 0 : island_hi;
   a.ext[0] = c->grid.n[0] + 2 * c->grid.ng;
   a.ext[1] = c->grid.n[1] + 2 * c->grid.ng;
   a.ext[2] = 1;
@@ -745,8 +875,8 @@ int pic_gr_metric_eval(pic_ctx* c, const pic_gr_metric* g, const double* x, int6
 }
 
 int pic_gr_push(pic_ctx* c, const pic_gr_metric* g, pic_species* sp, const void* em,
-                const void* em0, double dt, double omegaB0, int32_t niter, int32_t island_i1,
-                void* stream) {
+                const void* em0, double dt, double omegaB0, int32_t niter, int32_t island_lo,
+                int32_t island_hi, void* stream) {
   int st = gr_check(c, g);
   if (st != PIC_OK) return st;
   if (!em || !em0 || niter < 1) return PIC_ERR_ARG;
@@ -756,12 +886,14 @@ int pic_gr_push(pic_ctx* c, const pic_gr_metric* g, pic_species* sp, const void*
   if (sp->pusher == PIC_PUSHER_VAY) return PIC_ERR_UNSUPPORTED;
   if (sp->pusher == PIC_PUSHER_BORIS && sp->mass == 0.0f) return PIC_ERR_ARG;
   cudaStream_t s = strm(stream);
-  return is_f64(c) ? gr_push<double>(c, g, sp, em, em0, dt, omegaB0, niter, island_i1, s)
-                   : gr_push<float>(c, g, sp, em, em0, dt, omegaB0, niter, island_i1, s);
+  return is_f64(c)
+           ? gr_push<double>(c, g, sp, em, em0, dt, omegaB0, niter, island_lo, island_hi, s)
+           : gr_push<float>(c, g, sp, em, em0, dt, omegaB0, niter, island_lo, island_hi, s);
 }
 
 int pic_gr_deposit(pic_ctx* c, const pic_gr_metric* g, const pic_species* sp, int32_t nspecies,
-                   void* J, double dt, int32_t island_i1, uint32_t flags, void* stream) {
+                   void* J, double dt, int32_t island_lo, int32_t island_hi, uint32_t flags,
+                   void* stream) {
   int st = gr_check(c, g);
   if (st != PIC_OK) return st;
   if (!J || nspecies < 0 || (nspecies > 0 && !sp)) return PIC_ERR_ARG;
@@ -779,8 +911,8 @@ int pic_gr_deposit(pic_ctx* c, const pic_gr_metric* g, const pic_species* sp, in
   for (int k = 0; k < nspecies; ++k) {
     const pic_species* sk = sp + k;
     if (sk->npart == 0 || sk->pusher == PIC_PUSHER_NONE || sk->charge == 0.0f) continue;
-    st = is_f64(c) ? gr_deposit<double>(c, g, sk, J, dt, island_i1, s)
-                   : gr_deposit<float>(c, g, sk, J, dt, island_i1, s);
+    st = is_f64(c) ? gr_deposit<double>(c, g, sk, J, dt, island_lo, island_hi, s)
+                   : gr_deposit<float>(c, g, sk, J, dt, island_lo, island_hi, s);
     if (st != PIC_OK) return st;
   }
   return PIC_OK;

@@ -332,6 +332,11 @@ int pic_destroy(pic_ctx* c) {
   cudaFree(c->d_err);
   cudaFree(c->d_energy);
   if (c->sort_buf) cudaFree(c->sort_buf);
+  cudaFree(c->gr_island);
+  cudaFree(c->gr_island_cnt);
+  if (c->gr_fork) cudaEventDestroy(c->gr_fork);
+  if (c->gr_join) cudaEventDestroy(c->gr_join);
+  if (c->gr_side) cudaStreamDestroy(c->gr_side);
   pic::adjoint_release(c->adjoint);
   delete c;
   return PIC_OK;

@@ -72,16 +72,17 @@ class GRContext(Context):
                  _stream_ptr(stream))
         return out
 
-    def gr_push(self, sp: SpeciesArrays, em, em0, dt, omegaB0, niter=10, island_i1=0,
+    def gr_push(self, sp: SpeciesArrays, em, em0, dt, omegaB0, niter=10, island=(0, 0),
                 stream=None):
+        """island = (lo, hi): particles with lo <= i1 < hi push in FP64."""
         ps = make_species(sp, 2)
         abi.call("pic_gr_push", self.h, C.byref(self.m), C.byref(ps), _ptr(em), _ptr(em0), dt,
-                 omegaB0, niter, island_i1, _stream_ptr(stream))
+                 omegaB0, niter, island[0], island[1], _stream_ptr(stream))
 
-    def gr_deposit(self, species, J, dt, island_i1=0, zero=True, stream=None):
+    def gr_deposit(self, species, J, dt, island=(0, 0), zero=True, stream=None):
         arr = (abi.PicSpecies * len(species))(*[make_species(s, 2) for s in species])
         abi.call("pic_gr_deposit", self.h, C.byref(self.m), arr, len(species), _ptr(J), dt,
-                 island_i1, 0 if zero else abi.PIC_PD_NO_ZERO, _stream_ptr(stream))
+                 island[0], island[1], 0 if zero else abi.PIC_PD_NO_ZERO, _stream_ptr(stream))
 
     def gr_faraday(self, Bin, Bout, E, coeff, stream=None):
         abi.call("pic_gr_faraday", self.h, C.byref(self.m), _ptr(Bin), _ptr(Bout), _ptr(E), coeff,
@@ -115,13 +116,13 @@ class GRContext(Context):
                  _stream_ptr(stream))
         return out.value
 
-    def grpic_step(self, species, fields, prm, niter=10, island_i1=0, step=0, stream=None):
+    def grpic_step(self, species, fields, prm, niter=10, island=(0, 0), step=0, stream=None):
         """fields: list [em, em0, aux, cur, cur0, buff]; swapped in place like
         the reference's views."""
         arr = (abi.PicSpecies * len(species))(*[make_species(s, 2) for s in species])
         ptrs = (C.c_void_p * 6)(*[t.data_ptr() for t in fields])
         gp = abi.PicGRParams()
-        gp.niter, gp.island_i1 = niter, island_i1
+        gp.niter, gp.island_lo, gp.island_hi = niter, island[0], island[1]
         abi.call("pic_grpic_step", self.h, C.byref(self.m), arr, len(species), ptrs,
                  C.byref(prm), C.byref(gp), step, _stream_ptr(stream))
         by_ptr = {t.data_ptr(): t for t in fields}
@@ -131,9 +132,10 @@ class GRContext(Context):
 
 
 def horizon_island(g: GridSpec, spec: GRSpec, cells=3):
-    """First cell index beyond `cells` cells outside the horizon."""
-    x1h = spec.x1_of_r(g, spec.r_horizon)
-    return max(0, int(math.floor(x1h)) + 1 + cells)
+    """The FP64 island (lo, hi): the horizon's cell and `cells` cells on
+    either side of it, i1 in [lo, hi)."""
+    ih = int(math.floor(spec.x1_of_r(g, spec.r_horizon)))
+    return max(0, ih - cells), max(0, ih + 1 + cells)
 
 
 def gr_step_params(ctx: GRContext, *, cfl, ppc0, skindepth0, larmor0, sort_interval=0,

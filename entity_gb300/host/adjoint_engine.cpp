@@ -5,7 +5,8 @@
 // dead removal off so that particle indices stay fixed), with the full state
 // saved every K steps. Backward: for each K-step segment, newest first, the
 // segment is recomputed from its checkpoint with every step's starting state
-// kept, then walked backwards with pic_srpic_step_adjoint. Particle state is
+// kept, then walked backwards with pic_srpic_step_adjoint. The last segment
+// keeps its steps' states during the forward and is not recomputed. Particle state is
 // therefore stored for N/K checkpoints plus K snapshots, never per step of
 // the whole run.
 #include <algorithm>
@@ -65,10 +66,14 @@ extern "C" int pic_srpic_gradient(pic_ctx* ctx, pic_species* sp, pic_species_adj
 #define PIC_TRY(x)              \
   if ((st = (x)) != PIC_OK) \
     return st;
-  // forward with checkpoints
+  // forward with checkpoints; the steps of the last segment keep their
+  // starting states as they go, so that segment needs no recompute
+  const int64_t last0 = (nseg - 1) * every;
   for (int64_t n = 0; n < nsteps; ++n) {
     if (n % every == 0) PIC_TRY(pic_checkpoint_save(ctx, (int32_t)(n / every), sp, nsp, EB, stream));
     PIC_TRY(pic_srpic_step(ctx, sp, nsp, EB, J, buff, &p, n, stream));
+    if (n >= last0 && n + 1 < nsteps)
+      PIC_TRY(pic_checkpoint_save(ctx, (int32_t)(nseg + (n + 1 - last0)), sp, nsp, EB, stream));
   }
   double en[2];
   PIC_TRY(pic_field_energy(ctx, EB, p.dx, en, stream));
@@ -79,10 +84,12 @@ extern "C" int pic_srpic_gradient(pic_ctx* ctx, pic_species* sp, pic_species_adj
   std::vector<pic_species> view(nsp > 0 ? nsp : 1);
   for (int64_t seg = nseg - 1; seg >= 0; --seg) {
     const int64_t n0 = seg * every, n1 = std::min(nsteps, n0 + every);
-    PIC_TRY(pic_checkpoint_restore(ctx, (int32_t)seg, sp, nsp, EB, stream));
-    for (int64_t n = n0; n + 1 < n1; ++n) {
-      PIC_TRY(pic_srpic_step(ctx, sp, nsp, EB, J, buff, &p, n, stream));
-      PIC_TRY(pic_checkpoint_save(ctx, (int32_t)(nseg + (n + 1 - n0)), sp, nsp, EB, stream));
+    if (seg < nseg - 1) {
+      PIC_TRY(pic_checkpoint_restore(ctx, (int32_t)seg, sp, nsp, EB, stream));
+      for (int64_t n = n0; n + 1 < n1; ++n) {
+        PIC_TRY(pic_srpic_step(ctx, sp, nsp, EB, J, buff, &p, n, stream));
+        PIC_TRY(pic_checkpoint_save(ctx, (int32_t)(nseg + (n + 1 - n0)), sp, nsp, EB, stream));
+      }
     }
     for (int64_t n = n1 - 1; n >= n0; --n) {
       // the step's starting state is read in place from its slot

@@ -84,9 +84,11 @@ int gr_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, int32_t nsp, 
   for (int32_t k = 0; k < nsp; ++k) {
     if (sp[k].npart == 0 || sp[k].pusher == PIC_PUSHER_NONE) continue;
     PIC_TRY(pic_gr_push(ctx, m, sp + k, f[0], f[1], (double)dt, (double)(real)p.omegaB0,
-                        gp.niter, gp.island_i1, stream));
+                        gp.niter, gp.island_lo, gp.island_hi, stream));
   }
-  if (dep) PIC_TRY(pic_gr_deposit(ctx, m, sp, nsp, f[4], (double)dt, gp.island_i1, 0u, stream));
+  if (dep)
+    PIC_TRY(pic_gr_deposit(ctx, m, sp, nsp, f[4], (double)dt, gp.island_lo, gp.island_hi, 0u,
+                           stream));
   PIC_TRY(mark(PIC_PHASE_PUSH_DEPOSIT, 1));
   if (fs) {
     PIC_TRY(mark(PIC_PHASE_FIELDSOLVER, 0));

@@ -401,21 +401,24 @@ int pic_gr_metric_eval(pic_ctx* ctx, const pic_gr_metric* m, const double* x, in
 /* kernel::gr::Pusher_kernel (src/kernels/pushers/gr.hpp:664-865) for one
  * species: D interpolated from em, B from em0 at the grid's shape order
  * (1-3); Boris (massive) or photon; `niter` implicit iterations; prev arrays
- * written. In a single-precision build, particles with i1 < island_i1 run
- * the metric and both implicit iterations in double. The reference's
+ * written. In a single-precision build, particles with island_lo <= i1 <
+ * island_hi (the FP64 island: a band of cells around the horizon) run the
+ * metric and both implicit iterations in double; an empty band (island_hi <=
+ * island_lo) pushes every particle in single precision. The reference's
  * UpdatePhi takes phi by value (gr.hpp:459-480), so phi is never changed
  * there; it is not written here either. */
 int pic_gr_push(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, const void* em,
-                const void* em0, double dt, double omegaB0, int32_t niter, int32_t island_i1,
-                void* stream);
+                const void* em0, double dt, double omegaB0, int32_t niter, int32_t island_lo,
+                int32_t island_hi, void* stream);
 
 /* grpic::CurrentsDeposit (src/engines/grpic/currents.h:29-73): the current
  * of the last push at shape order 1 (hard-wired in the reference) with the
- * metric out-of-plane velocity (currents_deposit.hpp:138-159); J is zeroed
+ * metric out-of-plane velocity (currents_deposit.hpp:138-159), evaluated
+ * in double inside the FP64 island [island_lo, island_hi); J is zeroed
  * first unless flags has PIC_PD_NO_ZERO. */
 int pic_gr_deposit(pic_ctx* ctx, const pic_gr_metric* m, const pic_species* sp,
-                   int32_t nspecies, void* J, double dt, int32_t island_i1, uint32_t flags,
-                   void* stream);
+                   int32_t nspecies, void* J, double dt, int32_t island_lo, int32_t island_hi,
+                   uint32_t flags, void* stream);
 
 /* gr::Faraday_kernel (faraday_gr.hpp:31-102) over the active cells:
  * Bout = Bin + coeff * curl E (coeff = fraction * correction * dt; Bin may
@@ -456,7 +459,8 @@ int pic_gr_min_cell_size(pic_ctx* ctx, const pic_gr_metric* m, double* out, void
 /* GR step parameters beyond pic_step_params */
 typedef struct {
   int32_t niter;      /* pusher iterations (algorithms.gr.pusher_niter, default 10) */
-  int32_t island_i1;  /* particles with i1 below run the pusher in FP64 */
+  int32_t island_lo;  /* particles with island_lo <= i1 < island_hi run the */
+  int32_t island_hi;  /* pusher in FP64 (single-precision builds) */
 } pic_gr_params;
 
 /* GRPICEngine::step_forward (src/engines/grpic/grpic.hpp:66-634) on one

@@ -137,7 +137,7 @@ static void xi_to_i_di(real X, int* i, float* di) {
 
 void orc_gr_push(const orc_grid* g, const orc_qks* q, orc_species* sp, const void* em,
                  const void* em0, double dt_d, double omegaB0, int niter, int order,
-                 const int absorb[2], const int axis[2], int island_i1) {
+                 const int absorb[2], const int axis[2], int island_lo, int island_hi) {
   real*      u[3] = { (real*)sp->ux1, (real*)sp->ux2, (real*)sp->ux3 };
   const int  massive = sp->pusher != ORC_PUSHER_PHOTON;
   const real dt      = (real)dt_d;
@@ -156,10 +156,11 @@ void orc_gr_push(const orc_grid* g, const orc_qks* q, orc_species* sp, const voi
     if (massive) orc_interp2(g, em, em0, order, sp->i1[p], sp->i2[p], sp->dx1[p], sp->dx2[p], Dc, Bc);
     real xo[2], uo[3];
 #ifdef ORC_SINGLE
-    const int dbl = sp->i1[p] < island_i1;
+    const int dbl = sp->i1[p] >= island_lo && sp->i1[p] < island_hi;
 #else
     const int dbl = 1;
-    (void)island_i1;
+    (void)island_lo;
+    (void)island_hi;
 #endif
     if (dbl) {
       /* i_di_to_Xi in real_t, then the island's double arithmetic */
@@ -213,7 +214,7 @@ void orc_gr_push(const orc_grid* g, const orc_qks* q, orc_species* sp, const voi
 }
 
 void orc_gr_deposit(const orc_grid* g, const orc_qks* q, const orc_species* sp, void* J,
-                    double dt, int island_i1) {
+                    double dt, int island_lo, int island_hi) {
   if (sp->pusher == ORC_PUSHER_NONE || sp->npart == 0 || sp->charge == 0.0f) return;
   const real* u[3] = { (const real*)sp->ux1, (const real*)sp->ux2, (const real*)sp->ux3 };
   real*       vz   = (real*)calloc((size_t)sp->npart, sizeof(real));
@@ -222,10 +223,11 @@ void orc_gr_deposit(const orc_grid* g, const orc_qks* q, const orc_species* sp, 
   for (int64_t p = 0; p < sp->npart; ++p) {
     if (sp->tag[p] == ORC_TAG_DEAD) continue;
 #ifdef ORC_SINGLE
-    const int dbl = sp->i1[p] < island_i1;
+    const int dbl = sp->i1[p] >= island_lo && sp->i1[p] < island_hi;
 #else
     const int dbl = 1;
-    (void)island_i1;
+    (void)island_lo;
+    (void)island_hi;
 #endif
     if (dbl) {
       const double xp[2] = { (double)((real)sp->i1[p] + (real)sp->dx1[p]),

@@ -12,9 +12,9 @@
  * (theta = eta) is supported.
  *
  * Precision island: in the single-precision build, particles whose cell
- * satisfies i1 < island_i1 (the horizon cell + 3) run the metric and the
- * push iterations in double, as the product does; the double build runs
- * everything in double.
+ * satisfies island_lo <= i1 < island_hi (a band of cells around the
+ * horizon) run the metric and the push iterations in double, as the product
+ * does; the double build runs everything in double.
  */
 #ifndef ENTITY_GRPIC_ORACLE_H
 #define ENTITY_GRPIC_ORACLE_H
@@ -55,12 +55,12 @@ void orc_gr_transform(const orc_qks* q, int kind, const double* x, const double*
  * Writes i*_prev/dx*_prev. */
 void orc_gr_push(const orc_grid* g, const orc_qks* q, orc_species* sp, const void* em,
                  const void* em0, double dt, double omegaB0, int niter, int order,
-                 const int absorb[2], const int axis[2], int island_i1);
+                 const int absorb[2], const int axis[2], int island_lo, int island_hi);
 
 /* GR current deposit (currents_deposit.hpp, GR branch, shape order 1):
  * adds into J */
 void orc_gr_deposit(const orc_grid* g, const orc_qks* q, const orc_species* sp, void* J,
-                    double dt, int island_i1);
+                    double dt, int island_lo, int island_hi);
 
 /* field kernels; fields are 6-component (D or E in 0..2, B or H in 3..5)
  * Faraday_kernel (faraday_gr.hpp:31-102): Bout = Bin - curl E, over the

@@ -247,8 +247,8 @@ def _gr_sigs(L):
     L.orc_qks_init.argtypes = [Q, C.c_int, C.c_int, D, D, D, D, D, D, D]
     L.orc_gr_metric.argtypes = [Q, V, C.c_int64, V]
     L.orc_gr_transform.argtypes = [Q, C.c_int, V, V, C.c_int64, V]
-    L.orc_gr_push.argtypes = [G, Q, S, V, V, D, D, C.c_int, C.c_int, I2, I2, C.c_int]
-    L.orc_gr_deposit.argtypes = [G, Q, S, V, D, C.c_int]
+    L.orc_gr_push.argtypes = [G, Q, S, V, V, D, D, C.c_int, C.c_int, I2, I2, C.c_int, C.c_int]
+    L.orc_gr_deposit.argtypes = [G, Q, S, V, D, C.c_int, C.c_int]
     L.orc_gr_faraday.argtypes = [G, Q, V, V, V, D, C.c_int]
     L.orc_gr_ampere.argtypes = [G, Q, V, V, V, D, C.c_int, C.c_int]
     L.orc_gr_currents_ampere.argtypes = [G, Q, V, V, D, C.c_int, C.c_int]
@@ -286,19 +286,19 @@ class GROracle(Oracle):
         return out
 
     def gr_push(self, sp, em, em0, dt, omegaB0, niter=10, absorb=(1, 1), axis=(1, 1),
-                island_i1=0):
+                island=(0, 0)):
         s = self.species(sp)
         self.L.orc_gr_push(C.byref(self.og), C.byref(self.q), C.byref(s), _p(em), _p(em0), dt,
                            omegaB0, niter, self.g.order, (C.c_int * 2)(*absorb),
-                           (C.c_int * 2)(*axis), island_i1)
+                           (C.c_int * 2)(*axis), island[0], island[1])
 
-    def gr_deposit(self, species, J, dt, island_i1=0, zero=True):
+    def gr_deposit(self, species, J, dt, island=(0, 0), zero=True):
         if zero:
             J.zero_()
         for sp in species:
             s = self.species(sp)
             self.L.orc_gr_deposit(C.byref(self.og), C.byref(self.q), C.byref(s), _p(J), dt,
-                                  island_i1)
+                                  island[0], island[1])
 
     def gr_faraday(self, Bin, Bout, E, coeff, axis_min=1):
         self.L.orc_gr_faraday(C.byref(self.og), C.byref(self.q), _p(Bin), _p(Bout), _p(E), coeff,
@@ -331,7 +331,7 @@ class GROracle(Oracle):
     # GRPICEngine::step_forward (grpic.hpp:66-634), the sequence of the
     # product's engine: fields = [em, em0, aux, cur, cur0, buff], swapped in
     # place; axis/horizon boundaries on em and em0 after each update
-    def grpic_step(self, species, fields, prm, niter=10, island_i1=0, step=0, flags=(1, 1, 1)):
+    def grpic_step(self, species, fields, prm, niter=10, island=(0, 0), step=0, flags=(1, 1, 1)):
         R = self.g.real
         t = lambda v: torch.tensor(v, dtype=R)
         amin, amax, hor = flags
@@ -382,10 +382,9 @@ class GROracle(Oracle):
             self.gr_aux_h(em, em0, aux, amax)
         for sp in species:
             if sp.npart > 0 and sp.pusher != 0:
-                self.gr_push(sp, em, em0, float(dt), prm.omegaB0, niter,
-                             island_i1=island_i1)
+                self.gr_push(sp, em, em0, float(dt), prm.omegaB0, niter, island=island)
         if dep:
-            self.gr_deposit(species, fields[4], float(dt), island_i1=island_i1)
+            self.gr_deposit(species, fields[4], float(dt), island=island)
         if fs:
             cur, cur0 = fields[3], fields[4]
             if dep:

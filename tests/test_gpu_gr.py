@@ -88,10 +88,11 @@ def test_gr_push_matches_oracle(real, order, pusher):
     em, em0 = _rand_fields(g, 1), _rand_fields(g, 2)
     sp = _particles(g, 4000, 5, pusher=pusher)
     dt, omegaB0 = 0.05, 2.0
-    island = g.n[0] // 3
+    # a band away from both ends, so particles lie below, in and above it
+    island = (g.n[0] // 6, g.n[0] // 3)
     spg = sp.clone().to("cuda")
-    o.gr_push(sp, em, em0, dt, omegaB0, 10, island_i1=island)
-    ctx.gr_push(spg, em.cuda(), em0.cuda(), dt, omegaB0, 10, island_i1=island)
+    o.gr_push(sp, em, em0, dt, omegaB0, 10, island=island)
+    ctx.gr_push(spg, em.cuda(), em0.cuda(), dt, omegaB0, 10, island=island)
     torch.cuda.synchronize()
     assert ctx.device_errors() == [0, 0, 0, 0]
     assert torch.equal(sp.tag, spg.tag.cpu())
@@ -107,6 +108,29 @@ def test_gr_push_matches_oracle(real, order, pusher):
         assert float((a - b)[alive].abs().max()) <= tol * 10 * scale, c
 
 
+@pytest.mark.parametrize("band", [(0, 48), (8, 9), (30, 10)])
+def test_gr_push_island_bands(band):
+    """FP32 with the island band covering every cell (many more 32-particle
+    chunks than the island kernel has warps, so warps take several each),
+    one cell, and an empty band (hi < lo: everything in FP32)."""
+    g, spec, ctx, o = _setup(torch.float32, order=2)
+    em, em0 = _rand_fields(g, 1), _rand_fields(g, 2)
+    sp = _particles(g, 120000 if band == (0, 48) else 20000, 11)
+    spg = sp.clone().to("cuda")
+    o.gr_push(sp, em, em0, 0.05, 2.0, 10, island=band)
+    ctx.gr_push(spg, em.cuda(), em0.cuda(), 0.05, 2.0, 10, island=band)
+    torch.cuda.synchronize()
+    assert ctx.device_errors() == [0, 0, 0, 0]
+    assert torch.equal(sp.tag, spg.tag.cpu())
+    alive = sp.tag == 1
+    for d in range(2):
+        assert float((_X(sp, d) - _X(spg, d))[alive].abs().max()) <= TOL[torch.float32] * 50
+    for c in range(3):
+        a, b = sp.u[c].double(), spg.u[c].cpu().double()
+        scale = float(a.abs().max()) + 1e-30
+        assert float((a - b)[alive].abs().max()) <= TOL[torch.float32] * 10 * scale, c
+
+
 @pytest.mark.parametrize("real", REALS)
 def test_gr_deposit_matches_oracle(real):
     from entity_gb300.inputs import empty_field
@@ -114,12 +138,12 @@ def test_gr_deposit_matches_oracle(real):
     em, em0 = _rand_fields(g, 1, amp=0.02), _rand_fields(g, 2, amp=0.02)
     sp = _particles(g, 4000, 7)
     dt = 0.05
-    island = g.n[0] // 3
-    o.gr_push(sp, em, em0, dt, 2.0, 10, island_i1=island)   # sets the prev arrays
+    island = (g.n[0] // 6, g.n[0] // 3)
+    o.gr_push(sp, em, em0, dt, 2.0, 10, island=island)   # sets the prev arrays
     J = empty_field(g, 3)
-    o.gr_deposit([sp], J, dt, island_i1=island)
+    o.gr_deposit([sp], J, dt, island=island)
     Jg = empty_field(g, 3, "cuda")
-    ctx.gr_deposit([sp.clone().to("cuda")], Jg, dt, island_i1=island)
+    ctx.gr_deposit([sp.clone().to("cuda")], Jg, dt, island=island)
     torch.cuda.synchronize()
     assert ctx.device_errors() == [0, 0, 0, 0]
     scale = float(J.abs().max())
@@ -192,8 +216,8 @@ def test_grpic_step_matches_oracle(real):
     cpu_fields = [f.cpu().clone() for f in fields]
     cpu_species = [s.clone().to("cpu") for s in species]
     for step in range(5):
-        ctx.grpic_step(species, fields, prm, niter=10, island_i1=island, step=step)
-        o.grpic_step(cpu_species, cpu_fields, prm, niter=10, island_i1=island, step=step)
+        ctx.grpic_step(species, fields, prm, niter=10, island=island, step=step)
+        o.grpic_step(cpu_species, cpu_fields, prm, niter=10, island=island, step=step)
     torch.cuda.synchronize()
     assert ctx.device_errors() == [0, 0, 0, 0]
     # FP32: the current sums' order differs (atomics) and the step feeds J
@@ -261,6 +285,6 @@ def test_gr_magnetic_flux_stays_divergence_free(real):
     eps = 1e-5 if real == torch.float32 else 1e-12
     assert float(d0.abs().max()) <= eps * s0
     for step in range(10):
-        ctx.grpic_step(species, fields, prm, niter=10, island_i1=island, step=step)
+        ctx.grpic_step(species, fields, prm, niter=10, island=island, step=step)
     d1, s1 = div(fields[0])
     assert float(d1.abs().max()) <= 20 * eps * s1
