@@ -59,10 +59,12 @@ WORKLOADS = {
                       skindepth0=10.0, cfl=0.45, steps=400, every=20),
     # Kerr (a = 0.95) quasi-spherical Kerr-Schild grid, r log-spaced in
     # [0.9 r_h, 50 r_g], theta in [0, pi], vertical seed field, e-/e+ at rest
-    # 4 per cell in r < 6 r_g; FP32 with the pusher in FP64 within 3 cells of
-    # the horizon (either side)
+    # injected on the device, 4 pairs per cell on average in r < 6 r_g with
+    # weights sqrt(det h) / V0; FP32 with the pusher in FP64 within 3 cells
+    # of the horizon (either side)
     "wald2d": dict(name="2D GR Wald problem 1024(r) x 512(theta), a 0.95, vertical field, "
-                        "e-/e+ 4 ppc in r < 6, order 2, FP32 with FP64 near the horizon",
+                        "e-/e+ injected on the device, 4 pairs/cell in r < 6, order 2, FP32 with FP64 "
+                        "near the horizon",
                    dim=2, n=(1024, 512, 1), order=2, a=0.95, r_max=50.0, ppc=4, r_inject=6.0,
                    cfl=0.5, skindepth0=0.05, larmor0=0.0025, ppc0=2.0, niter=10,
                    sort_interval=0, clear_interval=100, precision_n=(512, 256),
@@ -601,11 +603,15 @@ def wald_precision(w, n, steps):
     (dead particles are not removed, so indices stay aligned)."""
     from entity_gb300.gr import gr_step_params, horizon_island, wald_setup
     runs = {}
+    # every run starts from the FP32 injection (a double injection draws
+    # 53-bit uniforms, i.e. other positions)
+    _, _, _, _, species32 = wald_setup(n=n, a=w["a"], r_max=w["r_max"], order=w["order"],
+                                       ppc=w["ppc"], r_inject=w["r_inject"], real=torch.float32)
     for tag, real, isl in (("f64", torch.float64, True), ("f32_island", torch.float32, True),
                            ("f32_no_island", torch.float32, False)):
-        g, spec, ctx, fields, species = wald_setup(n=n, a=w["a"], r_max=w["r_max"],
-                                                   order=w["order"], ppc=w["ppc"],
-                                                   r_inject=w["r_inject"], real=real)
+        g, spec, ctx, fields, _ = wald_setup(n=n, a=w["a"], r_max=w["r_max"], order=w["order"],
+                                             ppc=w["ppc"], r_inject=w["r_inject"], real=real)
+        species = [s.astype(real) for s in species32]
         prm = gr_step_params(ctx, cfl=w["cfl"], ppc0=w["ppc0"], skindepth0=w["skindepth0"],
                              larmor0=w["larmor0"], sort_interval=0, clear_interval=0)
         island = horizon_island(g, spec) if isl else (0, 0)

@@ -82,6 +82,13 @@ class PicGRMetric(C.Structure):
                 ("axis_min", C.c_int32), ("axis_max", C.c_int32), ("horizon", C.c_int32)]
 
 
+class PicInjectParams(C.Structure):
+    _fields_ = [("number_density", C.c_double), ("ppc0", C.c_double),
+                ("xi_min", C.c_double * 3), ("xi_max", C.c_double * 3),
+                ("temperature", C.c_double * 2), ("drift", (C.c_double * 3) * 2),
+                ("seed", C.c_uint64), ("first_pair", C.c_uint64)]
+
+
 class PicGRParams(C.Structure):
     _fields_ = [("niter", C.c_int32), ("island_lo", C.c_int32), ("island_hi", C.c_int32)]
 
@@ -129,6 +136,14 @@ SIGNATURES = {
     "pic_particle_moments": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32,
                                        C.POINTER(C.c_double), _VP]),
     "pic_charge_density": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32, _VP, _VP]),
+    "pic_inject_uniform_maxwellians": (C.c_int, [_VP, C.POINTER(PicSpecies),
+                                                 C.POINTER(PicSpecies),
+                                                 C.POINTER(PicInjectParams),
+                                                 C.POINTER(C.c_int64), _VP]),
+    "pic_gr_inject_uniform_maxwellians": (C.c_int, [_VP, C.POINTER(PicGRMetric),
+                                                    C.POINTER(PicSpecies), C.POINTER(PicSpecies),
+                                                    C.POINTER(PicInjectParams), C.c_double,
+                                                    C.POINTER(C.c_int64), _VP]),
     "pic_srpic_step": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32, _VP, _VP, _VP,
                                  C.POINTER(PicStepParams), C.c_int64, _VP]),
     "pic_checkpoint_save": (C.c_int, [_VP, C.c_int32, C.POINTER(PicSpecies), C.c_int32, _VP,

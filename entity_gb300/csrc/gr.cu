@@ -17,6 +17,7 @@
 
 #include "ctx_internal.cuh"
 #include "fields.cuh"
+#include "gr_host.cuh"
 #include "gr_metric.cuh"
 #include "pic_common.cuh"
 
@@ -696,30 +697,6 @@ __global__ void k_gr_dxmin(QKS<double> m, int n1, int n2, double* out) {
 namespace {
 
 using pic::QKS;
-
-int gr_check(const pic_ctx* c, const pic_gr_metric* g) {
-  if (!c || !g) return PIC_ERR_ARG;
-  if (c->grid.dim != 2) return PIC_ERR_UNSUPPORTED;
-  if (g->h != 0.0) return PIC_ERR_UNSUPPORTED;
-  if (!(g->x1min > g->r0) || !(g->x1max > g->x1min) || !(g->x2max > g->x2min)) return PIC_ERR_ARG;
-  if (!(g->a >= 0.0 && g->a < 1.0)) return PIC_ERR_ARG;
-  return PIC_OK;
-}
-
-// QKerrSchild's constructor (qkerr_schild.h:76-92) in real_t arithmetic
-template <typename real>
-QKS<double> make_qks(const pic_ctx* c, const pic_gr_metric* g) {
-  QKS<double> m;
-  const real  a = (real)g->a, r0 = (real)g->r0;
-  const real  chi_min = (real)std::log((real)g->x1min - r0);
-  const real  eta_min = (real)g->x2min;
-  const real  dchi    = ((real)std::log((real)g->x1max - r0) - chi_min) / (real)c->grid.n[0];
-  const real  deta    = ((real)g->x2max - eta_min) / (real)c->grid.n[1];
-  m.a = a, m.r0 = r0, m.h0 = (real)g->h, m.chi_min = chi_min, m.eta_min = eta_min;
-  m.dchi = dchi, m.deta = deta, m.dchi_inv = (real)1 / dchi, m.deta_inv = (real)1 / deta;
-  m.small_angle = (double)((real)0.5 * deta) < 1e-3;
-  return m;
-}
 
 template <typename real>
 pic::GRFld<real> fld_of(const pic_ctx* c, const pic_gr_metric* g) {

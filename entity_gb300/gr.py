@@ -4,7 +4,8 @@
 QKerrSchild parameters (pic_gr_metric) and exposes the phase functions of
 GRPICEngine::step_forward (src/engines/grpic/grpic.hpp:66-634) by their
 reference names. `wald_setup` builds the Wald problem's grid, vertical seed
-field and an injected pair plasma (the reference's wald pgen injects none).
+field and a pair plasma injected on the device (the reference's wald pgen
+injects none).
 Device memory is held in torch tensors; all computation runs in
 libentity_pic.so.
 """
@@ -110,6 +111,17 @@ class GRContext(Context):
     def gr_init_vertical(self, EB, stream=None):
         abi.call("pic_gr_init_vertical", self.h, C.byref(self.m), _ptr(EB), _stream_ptr(stream))
 
+    def gr_inject_uniform_maxwellians(self, sp1: SpeciesArrays, sp2: SpeciesArrays, params, V0,
+                                      stream=None):
+        """pic_gr_inject_uniform_maxwellians: covariant velocities, weight
+        sqrt(det h) / V0; returns the number of pairs."""
+        p1, p2 = make_species(sp1, 2), make_species(sp2, 2)
+        n = C.c_int64(0)
+        abi.call("pic_gr_inject_uniform_maxwellians", self.h, C.byref(self.m), C.byref(p1),
+                 C.byref(p2), C.byref(params), V0, C.byref(n), _stream_ptr(stream))
+        sp1.npart, sp2.npart = p1.npart, p2.npart
+        return n.value
+
     def gr_min_cell_size(self, stream=None):
         out = C.c_double(0)
         abi.call("pic_gr_min_cell_size", self.h, C.byref(self.m), C.byref(out),
@@ -189,7 +201,12 @@ def inject_pairs(g: GridSpec, spec: GRSpec, ppc: int, r_inject: float, seed: int
 def wald_setup(n=(1024, 512), a=0.95, r_max=50.0, order=2, ppc=4, r_inject=6.0,
                real=torch.float32, seed=5):
     """The Wald problem: QKerrSchild a, r in [0.9 r_h, r_max], theta in
-    [0, pi], vertical seed field, e-/e+ pairs at rest in r < r_inject."""
+    [0, pi], vertical seed field, and e-/e+ pairs at rest injected on the
+    device by pic_gr_inject_uniform_maxwellians: `ppc` pairs per cell on
+    average, uniform in code coordinates over r < r_inject, weights
+    sqrt(det h) / V0 (the reference's GR injection weights), V0 = sqrt(det h)
+    at the first cell centre; then one cell sort of each species."""
+    from .inputs import empty_species, inject_params
     g = gr_grid(n[0], n[1], order=order, real=real)
     spec = GRSpec(a=a, r_max=r_max)
     ctx = GRContext(g, spec)
@@ -197,5 +214,16 @@ def wald_setup(n=(1024, 512), a=0.95, r_max=50.0, order=2, ppc=4, r_inject=6.0,
     ctx.gr_init_vertical(em)
     fields = [em, torch.zeros_like(em), torch.zeros_like(em), empty_field(g, 3, "cuda"),
               empty_field(g, 3, "cuda"), empty_field(g, 3, "cuda")]
-    species = inject_pairs(g, spec, ppc, r_inject, seed)
+    x1_inj = min(float(g.n[0]), spec.x1_of_r(g, r_inject))
+    cap = int(math.ceil(ppc * x1_inj * g.n[1])) + 1
+    species = [empty_species(g, cap, charge=q, index=k + 1) for k, q in enumerate((-1.0, 1.0))]
+    V0 = float(ctx.metric_eval([[0.5, 0.5]])[0, 10])
+    # pairs = ppc0 * density / 2 per cell (ComputeNumInject) with ppc0 = 1
+    prm = inject_params(2.0 * ppc, 1.0, ((0.0, x1_inj), (0.0, float(g.n[1]))), (0.0, 0.0),
+                        seed=seed)
+    ctx.gr_inject_uniform_maxwellians(species[0], species[1], prm, V0)
+    # the injector places pairs in random order: one cell sort, as the
+    # reference's SortParticles would at step 0 with spatial sorting on
+    for sp in species:
+        ctx.sort(sp, abi.PIC_SORT_SPATIAL | abi.PIC_SORT_SKIP_PREV)
     return g, spec, ctx, fields, species

@@ -103,6 +103,34 @@ class SpeciesArrays:
                              self.charge, self.pusher, self.npart, self.index)
 
 
+def empty_species(g: GridSpec, capacity: int, *, mass=1.0, charge=-1.0, pusher=1, index=1,
+                  device="cuda") -> SpeciesArrays:
+    """A species with room for `capacity` particles and none alive yet (the
+    arrays an injector appends to)."""
+    z = lambda dt: torch.zeros(capacity, dtype=dt, device=device)
+    return SpeciesArrays([z(torch.int32) for _ in range(3)], [z(torch.float32) for _ in range(3)],
+                         [z(torch.int32) for _ in range(3)], [z(torch.float32) for _ in range(3)],
+                         [z(g.real) for _ in range(3)], z(g.real), z(torch.int16), mass, charge,
+                         pusher, 0, index)
+
+
+def inject_params(number_density, ppc0, box, temperature, drift=((0, 0, 0), (0, 0, 0)), seed=1,
+                  first_pair=0):
+    """pic_inject_params: box = ((lo, hi), ...) in cells per simulated axis,
+    temperature = (T1, T2) in m0 c^2, drift = two four-velocity 3-vectors."""
+    from .abi import PicInjectParams
+    p = PicInjectParams()
+    p.number_density, p.ppc0 = number_density, ppc0
+    for d, (lo, hi) in enumerate(box):
+        p.xi_min[d], p.xi_max[d] = lo, hi
+    for s in range(2):
+        p.temperature[s] = temperature[s]
+        for c in range(3):
+            p.drift[s][c] = drift[s][c]
+    p.seed, p.first_pair = seed, first_pair
+    return p
+
+
 def _uniform(shape, gen, device, dtype=torch.float64):
     return torch.rand(shape, generator=gen, device=device, dtype=dtype)
 

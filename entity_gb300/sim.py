@@ -177,6 +177,17 @@ class Context:
         arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
         abi.call("pic_charge_density", self.h, arr, len(species), _ptr(rho), _stream_ptr(stream))
 
+    def inject_uniform_maxwellians(self, sp1: SpeciesArrays, sp2: SpeciesArrays, params,
+                                   stream=None):
+        """pic_inject_uniform_maxwellians: appends the pairs to both species
+        (npart advances); returns the number of pairs."""
+        p1, p2 = make_species(sp1, self.g.dim), make_species(sp2, self.g.dim)
+        n = C.c_int64(0)
+        abi.call("pic_inject_uniform_maxwellians", self.h, C.byref(p1), C.byref(p2),
+                 C.byref(params), C.byref(n), _stream_ptr(stream))
+        sp1.npart, sp2.npart = p1.npart, p2.npart
+        return n.value
+
     def device_errors(self, reset=False, stream=None):
         out = (C.c_int64 * 4)()
         abi.call("pic_get_device_errors", self.h, out, int(reset), _stream_ptr(stream))

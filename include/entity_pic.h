@@ -253,7 +253,8 @@ int pic_charge_density(pic_ctx* ctx, const pic_species* sp, int32_t nspecies, vo
  * pusher, out[1] = alive particles whose cell lies outside the grid (skipped
  * by the pusher, reported by the sort), out[2] = particles whose deposit
  * stencil would leave the ghost layers (a step beyond the CFL limit; their
- * current is not deposited).
+ * current is not deposited), out[3] = injected pairs whose velocity sampler
+ * ran out of its rejection-loop bound.
  * Synchronises the stream. reset != 0 clears the counters. */
 int pic_get_device_errors(pic_ctx* ctx, int64_t out[4], int32_t reset, void* stream);
 
@@ -472,6 +473,49 @@ typedef struct {
 int pic_grpic_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, int32_t nspecies,
                    void* fields[6], const pic_step_params* prm, const pic_gr_params* gprm,
                    int64_t step, void* stream);
+
+/* ---- particle injection ------------------------------------------------ */
+
+/* Parameters of arch::InjectUniformMaxwellians (src/archetypes/utils.h:46-107)
+ * for one species pair. The box is in code units (cells from the first
+ * active cell) per simulated axis; the reference takes it in physical
+ * coordinates and maps it with DeduceRegion. */
+typedef struct {
+  double   number_density; /* total over the pair, in units of n0 */
+  double   ppc0;           /* particles.ppc0 */
+  double   xi_min[3];      /* injection box [xi_min, xi_max), code units */
+  double   xi_max[3];
+  double   temperature[2]; /* per species, m0 c^2 units (divided by the species' mass) */
+  double   drift[2][3];    /* drift four-velocities (Cartesian only) */
+  uint64_t seed;           /* Philox4x32-10 key */
+  uint64_t first_pair;     /* pair p draws from the stream first_pair + p */
+} pic_inject_params;
+
+/* arch::InjectUniform (src/archetypes/particle_injector.h:203-261) with
+ * kernel::UniformInjector_kernel (src/kernels/injectors.hpp:83-289) on a
+ * Cartesian SR grid: n = (long)(ppc0 number_density / 2 * box cells) pairs
+ * (ComputeNumInject, particle_injector.h:112-139). Each pair gets one uniform
+ * position shared by both species and a Maxwell-Juttner velocity per species
+ * (energy_dist.h:79-273: Box-Muller below temperature 0.5, the Sobol method
+ * above, then the flipping boost toward the drift), weight 1, tag alive. The
+ * particles are appended at each species' npart, which is advanced by n on
+ * return (*n_pairs = n). Random numbers come from a Philox4x32-10 stream per
+ * pair (counter-based, so independent of the launch shape); the reference's
+ * Kokkos XorShift streams have no portable counterpart. The prev arrays are
+ * not written. PIC_ERR_ARG if a species would exceed maxnpart, a mass is not
+ * positive or the box leaves the grid. A sampler loop that runs out of its
+ * iteration bound is counted in the error word's out[3]. */
+int pic_inject_uniform_maxwellians(pic_ctx* ctx, pic_species* sp1, pic_species* sp2,
+                                   const pic_inject_params* prm, int64_t* n_pairs, void* stream);
+
+/* The same on the 2D QKerrSchild grid (the GRPIC branch of
+ * UniformInjector_kernel): the tetrad-frame sample is transformed to
+ * covariant components (transform<Idx::T, Idx::D>) at the particle, and the
+ * weight is sqrt(det h) / V0 there. The reference ignores a drift outside
+ * Cartesian coordinates; here a nonzero drift returns PIC_ERR_UNSUPPORTED. */
+int pic_gr_inject_uniform_maxwellians(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp1,
+                                      pic_species* sp2, const pic_inject_params* prm, double V0,
+                                      int64_t* n_pairs, void* stream);
 
 #ifdef __cplusplus
 }

@@ -4,6 +4,7 @@
  * reference kernel in its operation order.
  */
 #include "grpic_oracle.h"
+#include "inject_oracle.h"
 
 #include <float.h>
 #include <math.h>
@@ -540,4 +541,46 @@ void orc_gr_field_bcs(const orc_grid* g, void* fld_, int set_e, int set_b, int a
             F[EBI(g, i1min - ng + i, i2, c)] = F[EBI(g, i1min + 1 + nfilter, i2, c)];
     }
   }
+}
+
+/* the GRPIC branch of UniformInjector_kernel (injectors.hpp:230-239): the
+ * tetrad-frame sample transformed to covariant components at the particle
+ * (transform<Idx::T, Idx::D>), weight sqrt(det h) / V0 there */
+int64_t orc_gr_inject_uniform(const orc_grid* g, const orc_qks* q, orc_species* sp1,
+                              orc_species* sp2, const orc_inject_params* ip, double V0,
+                              int64_t* failures) {
+  const MT      m       = MK(q);
+  const int64_t n       = orc_inject_count(2, ip);
+  const float   mass[2] = { sp1->mass, sp2->mass };
+  orc_species*  sps[2]  = { sp1, sp2 };
+  const mreal   inv_V0  = (mreal)1 / (mreal)V0;
+  int64_t       bad     = 0;
+  (void)g;
+  for (int64_t p = 0; p < n; ++p) {
+    real x[3] = { 0, 0, 0 }, v[6];
+    if (!orc_inject_sample_pair(2, ip, mass, (uint64_t)p, x, v)) ++bad;
+    const mreal xp[2] = { (mreal)x[0], (mreal)x[1] };
+    const mreal w     = M_(sqrt_det_h)(&m, xp) * inv_V0;
+    for (int s = 0; s < 2; ++s) {
+      orc_species*  S = sps[s];
+      const int64_t k = S->npart + p;
+      const mreal   vt[3] = { (mreal)v[3 * s], (mreal)v[3 * s + 1], (mreal)v[3 * s + 2] };
+      mreal         vd[3];
+      M_(t_to_d)(&m, xp, vt, vd);
+      const int i1 = (int)x[0], i2 = (int)x[1];
+      S->i1[k]  = i1;
+      S->i2[k]  = i2;
+      S->dx1[k] = (float)(x[0] - (real)i1);
+      S->dx2[k] = (float)(x[1] - (real)i2);
+      ((real*)S->ux1)[k]    = (real)vd[0];
+      ((real*)S->ux2)[k]    = (real)vd[1];
+      ((real*)S->ux3)[k]    = (real)vd[2];
+      ((real*)S->weight)[k] = (real)w;
+      S->tag[k]             = ORC_TAG_ALIVE;
+    }
+  }
+  sp1->npart += n;
+  sp2->npart += n;
+  if (failures) *failures = bad;
+  return n;
 }

@@ -19,6 +19,7 @@
 #ifndef ENTITY_GRPIC_ORACLE_H
 #define ENTITY_GRPIC_ORACLE_H
 
+#include "inject_oracle.h"
 #include "srpic_oracle.h"
 
 #ifdef __cplusplus
@@ -88,6 +89,13 @@ void orc_gr_average_j(const orc_grid* g, void* J, const void* J0);
  * set_b select the components (D/E and B/H) */
 void orc_gr_field_bcs(const orc_grid* g, void* fld, int set_e, int set_b, int axis_min,
                       int axis_max, int horizon, int nfilter);
+
+/* the uniform Maxwellian pair injection on the QKerrSchild grid
+ * (inject_oracle.h for the random numbers): covariant velocities, weight
+ * sqrt(det h) / V0 */
+int64_t orc_gr_inject_uniform(const orc_grid* g, const orc_qks* q, orc_species* sp1,
+                              orc_species* sp2, const orc_inject_params* ip, double V0,
+                              int64_t* failures);
 
 #ifdef __cplusplus
 }

@@ -36,6 +36,39 @@ class OrcSpecies(C.Structure):
 _libs = {}
 
 
+class OrcInjectParams(C.Structure):
+    _fields_ = [("number_density", C.c_double), ("ppc0", C.c_double),
+                ("xi_min", C.c_double * 3), ("xi_max", C.c_double * 3),
+                ("temperature", C.c_double * 2), ("drift", (C.c_double * 3) * 2),
+                ("seed", C.c_uint64), ("first_pair", C.c_uint64)]
+
+
+def inject_params(number_density, ppc0, box, temperature, drift=((0, 0, 0), (0, 0, 0)), seed=1,
+                  first_pair=0, cls=None):
+    """Fills an injection parameter struct (the oracle's or, with cls, the
+    product's identical layout); box = ((lo, hi), ...) per simulated axis."""
+    p = (cls or OrcInjectParams)()
+    p.number_density, p.ppc0 = number_density, ppc0
+    for d, (lo, hi) in enumerate(box):
+        p.xi_min[d], p.xi_max[d] = lo, hi
+    for s in range(2):
+        p.temperature[s] = temperature[s]
+        for c in range(3):
+            p.drift[s][c] = drift[s][c]
+    p.seed, p.first_pair = seed, first_pair
+    return p
+
+
+def philox4x32_10(ctr, key):
+    """One Philox4x32-10 block of the oracle (four uint32 words)."""
+    L = lib(torch.float64)
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    L.orc_philox4x32_10(c, k, o)
+    return list(o)
+
+
 def lib(real):
     tag = "f32" if real == torch.float32 else "f64"
     if tag not in _libs:
@@ -65,6 +98,13 @@ def lib(real):
         L.orc_particle_moments.argtypes = [S, C.POINTER(C.c_double)]
         L.orc_max_threads.restype = C.c_int
         L.orc_real_size.restype = C.c_int
+        P = C.POINTER(OrcInjectParams)
+        U32 = C.POINTER(C.c_uint32)
+        L.orc_philox4x32_10.argtypes = [U32, U32, U32]
+        L.orc_inject_count.restype = C.c_int64
+        L.orc_inject_count.argtypes = [C.c_int, P]
+        L.orc_inject_uniform.restype = C.c_int64
+        L.orc_inject_uniform.argtypes = [G, S, S, P, C.POINTER(C.c_int64)]
         _libs[tag] = L
     return _libs[tag]
 
@@ -104,6 +144,16 @@ class Oracle:
         os_.weight, os_.tag = _p(sp.w), _p(sp.tag)
         os_.npart, os_.mass, os_.charge, os_.pusher = sp.npart, sp.mass, sp.charge, sp.pusher
         return os_
+
+    def inject_uniform(self, sp1, sp2, params):
+        """Appends the injected pairs (both species' npart advance); returns
+        (pairs, sampler failures)."""
+        s1, s2 = self.species(sp1), self.species(sp2)
+        bad = C.c_int64(0)
+        n = self.L.orc_inject_uniform(C.byref(self.og), C.byref(s1), C.byref(s2),
+                                      C.byref(params), C.byref(bad))
+        sp1.npart, sp2.npart = s1.npart, s2.npart
+        return n, bad.value
 
     def push(self, sp, EB, dt, omegaB0, dx):
         s = self.species(sp)
@@ -257,6 +307,9 @@ def _gr_sigs(L):
     L.orc_gr_average_db.argtypes = [G, V, V]
     L.orc_gr_average_j.argtypes = [G, V, V]
     L.orc_gr_field_bcs.argtypes = [G, V, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.orc_gr_inject_uniform.restype = C.c_int64
+    L.orc_gr_inject_uniform.argtypes = [G, Q, S, S, C.POINTER(OrcInjectParams), D,
+                                        C.POINTER(C.c_int64)]
     L._gr_ready = True
     return L
 
@@ -270,6 +323,14 @@ class GROracle(Oracle):
         self.q = OrcQKS()
         self.L.orc_qks_init(C.byref(self.q), g.n[0], g.n[1], r_min, r_max, th_min, th_max, a,
                             r0, h)
+
+    def gr_inject_uniform(self, sp1, sp2, params, V0):
+        s1, s2 = self.species(sp1), self.species(sp2)
+        bad = C.c_int64(0)
+        n = self.L.orc_gr_inject_uniform(C.byref(self.og), C.byref(self.q), C.byref(s1),
+                                         C.byref(s2), C.byref(params), V0, C.byref(bad))
+        sp1.npart, sp2.npart = s1.npart, s2.npart
+        return n, bad.value
 
     def metric(self, x):
         x = torch.as_tensor(x, dtype=torch.float64).contiguous()
