@@ -43,12 +43,13 @@ WORKLOADS = {
                         "4 filter passes, FP32", dim=3, n=(256, 256, 256), order=2, ppc=8,
                    temp=0.09, drift=0.0, nfilter=4, cfl=0.45, skindepth0=10.0, larmor0=10.0,
                    ppc0=16.0, field="turbulent", modes=8, dB=1.0, sample_n=(64, 64, 64),
-                   precision_n=(64, 64, 64), precision_steps=200, sort_interval=8),
+                   precision_n=(64, 64, 64), precision_steps=200, sort_interval=8,
+                   bench_steps=8),
     "pair2d": dict(name="2D SR pair plasma 512^2, e-/e+ 16 ppc each, drift +-0.3c, order 1, FP32",
                    dim=2, n=(512, 512, 1), order=1, ppc=16, temp=0.01, drift=0.3, nfilter=0,
                    cfl=0.45, skindepth0=10.0, larmor0=10.0, ppc0=16.0, field="none", modes=0,
                    dB=0.0, sample_n=(128, 128, 1), precision_n=(512, 512, 1),
-                   precision_steps=100, sort_interval=16),
+                   precision_steps=100, sort_interval=16, bench_steps=16),
     # magnetized uniform plasma: sigma = (skin depth / Larmor radius)^2 = 10,
     # Maxwell-Juttner theta = 1, uniform B0 along x3
     # two cold beams at +-0.2c (16 ppc each) with weights 1 + 1e-3 cos(k x),
@@ -554,7 +555,8 @@ def run_wald(args, w):
     island = horizon_island(g, spec)
     npart0 = sum(s.npart for s in species)
     for k in range(args.warmup):
-        ctx.grpic_step(species, fields, prm, niter=w["niter"], island=island, step=k)
+        ctx.grpic_step(species, fields, prm, niter=w["niter"], island=island, step=k,
+                       match=ctx.match)
     torch.cuda.synchronize()
     ctx.timers(True)
     sampler = ClockSampler(local)
@@ -567,7 +569,7 @@ def run_wald(args, w):
         steps_particles += sum(s.npart for s in species)
         a.record()
         ctx.grpic_step(species, fields, prm, niter=w["niter"], island=island,
-                       step=args.warmup + k)
+                       step=args.warmup + k, match=ctx.match)
         b.record()
         ev.append((a, b))
     torch.cuda.synchronize()
@@ -583,7 +585,8 @@ def run_wald(args, w):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": w["name"], "cells": n[0] * n[1], "particles_initial": npart0,
                    "particles_final": sum(s.npart for s in species), "dt": prm.dt,
-                   "fp64_island_cells": list(island), "parallelism": "replicas x1"},
+                   "fp64_island_cells": list(island), "match_ds": ctx.match[0],
+                   "parallelism": "replicas x1"},
         "ns_per_particle_step": 1e9 / value,
         "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in phases.items()},
         "device_errors": errs,
@@ -616,7 +619,8 @@ def wald_precision(w, n, steps):
                              larmor0=w["larmor0"], sort_interval=0, clear_interval=0)
         island = horizon_island(g, spec) if isl else (0, 0)
         for k in range(steps):
-            ctx.grpic_step(species, fields, prm, niter=w["niter"], island=island, step=k)
+            ctx.grpic_step(species, fields, prm, niter=w["niter"], island=island, step=k,
+                           match=ctx.match)
         torch.cuda.synchronize()
         ng = g.ng
         em = fields[0][:, 0, ng:ng + n[1], ng:ng + n[0]].double()
@@ -697,7 +701,9 @@ def run_sweep(args, w):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: the workload's, a multiple of its sort "
+                         "interval so that the window holds its share of sorts)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="turb3d", choices=sorted(WORKLOADS))
@@ -722,6 +728,8 @@ def main():
     w = WORKLOADS[args.workload]
     if args.sort_interval is None:
         args.sort_interval = w.get("sort_interval", 4)
+    if args.steps is None:
+        args.steps = w.get("bench_steps", 10)
     if args.cells is not None:
         c = list(args.cells) + [1] * (3 - len(args.cells))
         args.cells = tuple(c)

@@ -90,7 +90,8 @@ class PicInjectParams(C.Structure):
 
 
 class PicGRParams(C.Structure):
-    _fields_ = [("niter", C.c_int32), ("island_lo", C.c_int32), ("island_hi", C.c_int32)]
+    _fields_ = [("niter", C.c_int32), ("island_lo", C.c_int32), ("island_hi", C.c_int32),
+                ("match_ds", C.c_double), ("match_target", C.c_void_p)]
 
 
 class PicStepParams(C.Structure):
@@ -163,6 +164,9 @@ SIGNATURES = {
     "pic_gr_metric_eval": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, C.c_int64, _VP, _VP]),
     "pic_gr_push": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.POINTER(PicSpecies), _VP, _VP,
                               C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_int32, _VP]),
+    "pic_gr_particle_push": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.POINTER(PicSpecies),
+                                       C.c_int32, _VP, _VP, C.c_double, C.c_double, C.c_int32,
+                                       C.c_int32, C.c_int32, _VP]),
     "pic_gr_deposit": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.POINTER(PicSpecies), C.c_int32,
                                  _VP, C.c_double, C.c_int32, C.c_int32, C.c_uint32, _VP]),
     "pic_gr_faraday": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP, _VP, C.c_double, _VP]),
@@ -174,6 +178,9 @@ SIGNATURES = {
     "pic_gr_field_bcs": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, C.c_int32, C.c_int32,
                                    C.c_int32, _VP]),
     "pic_gr_init_vertical": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP]),
+    "pic_gr_match_fields": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP, C.c_double,
+                                      C.c_int32, C.c_int32, _VP]),
+    "pic_gr_absorb_currents": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, C.c_double, _VP]),
     "pic_gr_min_cell_size": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.POINTER(C.c_double),
                                        _VP]),
     "pic_grpic_step": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.POINTER(PicSpecies), C.c_int32,

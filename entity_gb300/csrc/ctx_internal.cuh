@@ -45,16 +45,18 @@ struct pic_ctx {
   std::vector<cudaEvent_t>                        event_pool;
   // checkpoint and snapshot storage of pic_srpic_gradient (grown on demand)
   pic::AdjointScratch*                            adjoint = nullptr;
-  // indices of the GR pusher's FP64-island particles followed by their
-  // membership bitmask (grown on demand), and two counters: the list length
-  // and the island kernel's work cursor
+  // indices of the GR pusher's FP64-island particles, species by species,
+  // followed by their membership bitmasks (grown on demand), and two
+  // counters per species: the list length and the island kernel's cursor
   int32_t*                                        gr_island     = nullptr;
-  int64_t                                         gr_island_cap = 0;
+  int64_t                                         gr_island_cap = 0;  // 32-bit words
   unsigned*                                       gr_island_cnt = nullptr;
-  // second stream of the island kernel, forked from and joined to the
-  // caller's stream by the two events
-  cudaStream_t                                    gr_side = nullptr;
-  cudaEvent_t                                     gr_fork = nullptr, gr_join = nullptr;
+  int                                             gr_island_nsp = 0;  // species of the counters
+  // per species, the stream of its island kernel and the event that joins it
+  // back to the caller's stream; one fork event for all
+  std::vector<cudaStream_t>                       gr_side;
+  std::vector<cudaEvent_t>                        gr_join;
+  cudaEvent_t                                     gr_fork = nullptr;
 };
 
 namespace pic_internal {

@@ -13,7 +13,9 @@
 //     the axis / horizon boundaries (fields_bcs.hpp:825-868, 1188-1240).
 // Metric values are evaluated at the staggered points they are needed at;
 // one thread per particle or per cell.
+#include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "ctx_internal.cuh"
 #include "fields.cuh"
@@ -369,7 +371,7 @@ __global__ void __launch_bounds__(256) k_gr_deposit(GRDepArgs<real> a) {
 // ---------------------------------------------------------------------------
 struct Range2 {
   int i0, i1, j0, j1;  // [i0, i1) x [j0, j1), ghost-inclusive indices
-  __device__ __forceinline__ int64_t count() const { return (int64_t)(i1 - i0) * (j1 - j0); }
+  __host__ __device__ __forceinline__ int64_t count() const { return (int64_t)(i1 - i0) * (j1 - j0); }
 };
 
 #define GR_CELL_LOOP(R)                                                                    \
@@ -621,6 +623,60 @@ __global__ void k_gr_horizon(GRFld<real> f, FieldView<real> F, int set_e, int se
   }
 }
 
+// MatchBoundaries_kernel, GRPIC branch in 2D with o = x1 (fields_bcs.hpp:
+// 181-340) over the cells of the +r layer: each component relaxes toward the
+// target field T (the problem generator's field, which the caller stores),
+// F = s F + (1 - s) T with s = tanh(4 |r - r_edge| / ds) at the component's
+// radius (i + 1/2 for D^r, B^theta, B^phi; i for D^theta, D^phi, B^r). On
+// the axis rows D^phi only decays (its target term is skipped there).
+template <typename real>
+__global__ void k_gr_match(GRFld<real> f, Range2 R, FieldView<real> F, FieldView<real> T,
+                           real r_edge, real ds, int set_e, int set_b) {
+  const QKS<real> m = f.m.template as<real>();
+  const real      H = 0.5, ONE = 1, FOUR = 4;
+  const int       N2 = f.n2 + 2 * f.ng;
+  auto shape = [&](real x1) {
+    const real r = m.r0 + mexp(x1 * m.dchi + m.chi_min);
+    return (real)tanh(fabs(r - r_edge) * FOUR / ds);
+  };
+  GR_CELL_LOOP(R)
+    const real i1_ = (real)(i1 - f.ng);
+    const real sH = shape(i1_ + H), s0 = shape(i1_);
+    auto blend = [&](int c, real sc) {
+      real& v = F.p[F.idx(i1, i2, 0, c)];
+      v = sc * v + (ONE - sc) * T.p[T.idx(i1, i2, 0, c)];
+    };
+    if (set_e) {
+      blend(0, sH);
+      blend(1, s0);
+      real& v = F.p[F.idx(i1, i2, 0, 2)];
+      v = s0 * v;
+      if ((!f.axis_min || i2 > f.ng) && (!f.axis_max || i2 < N2 - f.ng))
+        v += (ONE - s0) * T.p[T.idx(i1, i2, 0, 2)];
+    }
+    if (set_b) {
+      blend(3, s0);
+      blend(4, sH);
+      blend(5, sH);
+    }
+  }
+}
+
+// gr::AbsorbCurrents_kernel<M, 1> (fields_bcs.hpp:1243-1280) over the same
+// layer: J *= tanh(|r(i) - r_edge| / (ds / 4)), every component at r(i)
+template <typename real>
+__global__ void k_gr_absorb_currents(GRFld<real> f, Range2 R, FieldView<real> J, real r_edge,
+                                     real ds) {
+  const QKS<real> m = f.m.template as<real>();
+  const real      INV_4 = 0.25;
+  GR_CELL_LOOP(R)
+    const real i1_ = (real)(i1 - f.ng);
+    const real r   = m.r0 + mexp(i1_ * m.dchi + m.chi_min);
+    const real t   = (real)tanh(fabs(r - r_edge) / (INV_4 * ds));
+    for (int c = 0; c < 3; ++c) J.p[J.idx(i1, i2, 0, c)] *= t;
+  }
+}
+
 // metric functions at points (tests and diagnostics)
 template <typename real>
 __global__ void k_gr_metric_eval(QKS<double> md, const double* x, int64_t n, double* out) {
@@ -721,34 +777,47 @@ pic::Range2 active(const pic_ctx* c) {
   return pic::Range2{ ng, c->grid.n[0] + ng, ng, c->grid.n[1] + ng };
 }
 
-// the island list's buffers, the side stream and its events, made on first use
-int island_resources(pic_ctx* c, int64_t npart) {
-  if (!c->gr_island_cnt &&
-      cudaMalloc((void**)&c->gr_island_cnt, 2 * sizeof(unsigned)) != cudaSuccess)
-    return PIC_ERR_NOMEM;
-  if (c->gr_island_cap < npart) {
+// the island lists and masks of nsp species (list k: npart_k entries at
+// offset off_k; mask k: ceil(npart_k / 32) words after all lists), two
+// counters per species, one side stream and join event per species; made or
+// grown on first use
+int island_resources(pic_ctx* c, int nsp, int64_t words) {
+  if (c->gr_island_nsp < nsp) {
+    cudaFree(c->gr_island_cnt);
+    c->gr_island_cnt = nullptr;
+    c->gr_island_nsp = 0;
+    if (cudaMalloc((void**)&c->gr_island_cnt, 2 * sizeof(unsigned) * nsp) != cudaSuccess)
+      return PIC_ERR_NOMEM;
+    c->gr_island_nsp = nsp;
+  }
+  if (c->gr_island_cap < words) {
     cudaFree(c->gr_island);
     c->gr_island     = nullptr;
     c->gr_island_cap = 0;
-    // the list (npart entries) followed by the mask (one bit per particle)
-    const int64_t words = npart + (npart + 31) / 32;
     if (cudaMalloc((void**)&c->gr_island, sizeof(int32_t) * words) != cudaSuccess)
       return PIC_ERR_NOMEM;
-    c->gr_island_cap = npart;
+    c->gr_island_cap = words;
   }
-  if (!c->gr_side && cudaStreamCreateWithFlags(&c->gr_side, cudaStreamNonBlocking) != cudaSuccess)
-    return PIC_ERR_CUDA;
   if (!c->gr_fork && cudaEventCreateWithFlags(&c->gr_fork, cudaEventDisableTiming) != cudaSuccess)
     return PIC_ERR_CUDA;
-  if (!c->gr_join && cudaEventCreateWithFlags(&c->gr_join, cudaEventDisableTiming) != cudaSuccess)
-    return PIC_ERR_CUDA;
+  while ((int)c->gr_side.size() < nsp) {
+    cudaStream_t st = nullptr;
+    cudaEvent_t  ev = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return PIC_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+      cudaStreamDestroy(st);
+      return PIC_ERR_CUDA;
+    }
+    c->gr_side.push_back(st);
+    c->gr_join.push_back(ev);
+  }
   return PIC_OK;
 }
 
 template <typename real>
-int gr_push(pic_ctx* c, const pic_gr_metric* g, const pic_species* sp, const void* em,
-            const void* em0, double dt, double omegaB0, int32_t niter, int32_t island_lo,
-            int32_t island_hi, cudaStream_t s) {
+pic::GRPushArgs<real> push_args(pic_ctx* c, const pic_gr_metric* g, const pic_species* sp,
+                                const void* em, const void* em0, double dt, double omegaB0,
+                                int32_t niter, int32_t island_lo, int32_t island_hi) {
   pic::GRPushArgs<real> a;
   a.sp  = sptrs(sp);
   a.em  = em_view<real>(c, em);
@@ -770,47 +839,74 @@ int gr_push(pic_ctx* c, const pic_gr_metric* g, const pic_species* sp, const voi
   a.list       = nullptr;
   a.list_count = nullptr;
   a.mask       = nullptr;
+  return a;
+}
+
+// grpic::ParticlePush over the species sp[0..nsp) with npart > 0 and a
+// pusher (validated by the caller). FP32 with an island: the island lists
+// of all species are built first, then every species' island kernel runs on
+// its own side stream while the bulks run on s, and s waits for all of them.
+// The islands are latency-bound chains of FP64 work, so running them at once
+// costs little more than one.
+template <typename real>
+int gr_push_species(pic_ctx* c, const pic_gr_metric* g, const pic_species* const* sp, int nsp,
+                    const void* em, const void* em0, double dt, double omegaB0, int32_t niter,
+                    int32_t island_lo, int32_t island_hi, cudaStream_t s) {
   if (c->grid.order < 1 || c->grid.order > 3) return PIC_ERR_UNSUPPORTED;
-  const unsigned b     = blocks_for(sp->npart);
-  auto           bulk  = [&]() {
+  std::vector<pic::GRPushArgs<real>> a(nsp);
+  for (int k = 0; k < nsp; ++k)
+    a[k] = push_args<real>(c, g, sp[k], em, em0, dt, omegaB0, niter, island_lo, island_hi);
+  auto bulk = [&](const pic::GRPushArgs<real>& ak) {
+    const unsigned b = blocks_for(ak.sp.npart);
     switch (c->grid.order) {
-      case 1: PIC_KL(pic::k_gr_push<1, real><<<b, 256, 0, s>>>(a)); break;
-      case 2: PIC_KL(pic::k_gr_push<2, real><<<b, 256, 0, s>>>(a)); break;
-      default: PIC_KL(pic::k_gr_push<3, real><<<b, 256, 0, s>>>(a)); break;
+      case 1: PIC_KL(pic::k_gr_push<1, real><<<b, 256, 0, s>>>(ak)); break;
+      case 2: PIC_KL(pic::k_gr_push<2, real><<<b, 256, 0, s>>>(ak)); break;
+      default: PIC_KL(pic::k_gr_push<3, real><<<b, 256, 0, s>>>(ak)); break;
     }
   };
   // double fields run everything in double: no split
   if (sizeof(real) == 8 || island_hi <= island_lo) {
-    bulk();
+    for (int k = 0; k < nsp; ++k) bulk(a[k]);
     return cuda_status(cudaGetLastError());
   }
-  // the island list holds 32-bit particle indices
-  if (sp->npart > (int64_t)INT32_MAX) return PIC_ERR_UNSUPPORTED;
-  int st = island_resources(c, sp->npart);
-  if (st != PIC_OK) return st;
-  a.list       = c->gr_island;
-  a.list_count = c->gr_island_cnt;
-  a.mask       = reinterpret_cast<unsigned*>(c->gr_island + c->gr_island_cap);
-  if (cudaMemsetAsync(c->gr_island_cnt, 0, 2 * sizeof(unsigned), s) != cudaSuccess)
-    return PIC_ERR_CUDA;
-  PIC_KL(pic::k_gr_island_list<real><<<b, 256, 0, s>>>(a));
-  // fork: the island on the side stream beside the bulk on s; join
-  if (cudaEventRecord(c->gr_fork, s) != cudaSuccess ||
-      cudaStreamWaitEvent(c->gr_side, c->gr_fork, 0) != cudaSuccess)
-    return PIC_ERR_CUDA;
-  if constexpr (sizeof(real) == 4) {
-    // three 128-thread blocks per SM fit at up to 170 registers per thread
-    const unsigned bi = 152 * 3;
-    cudaStream_t   s2 = c->gr_side;
-    switch (c->grid.order) {
-      case 1: PIC_KL(pic::k_gr_push_island<1, real><<<bi, 128, 0, s2>>>(a)); break;
-      case 2: PIC_KL(pic::k_gr_push_island<2, real><<<bi, 128, 0, s2>>>(a)); break;
-      default: PIC_KL(pic::k_gr_push_island<3, real><<<bi, 128, 0, s2>>>(a)); break;
-    }
+  int64_t lists = 0, masks = 0;
+  for (int k = 0; k < nsp; ++k) {
+    // the island lists hold 32-bit particle indices
+    if (sp[k]->npart > (int64_t)INT32_MAX) return PIC_ERR_UNSUPPORTED;
+    lists += sp[k]->npart;
+    masks += (sp[k]->npart + 31) / 32;
   }
-  if (cudaEventRecord(c->gr_join, c->gr_side) != cudaSuccess) return PIC_ERR_CUDA;
-  bulk();
-  if (cudaStreamWaitEvent(s, c->gr_join, 0) != cudaSuccess) return PIC_ERR_CUDA;
+  int st = island_resources(c, nsp, lists + masks);
+  if (st != PIC_OK) return st;
+  if (cudaMemsetAsync(c->gr_island_cnt, 0, 2 * sizeof(unsigned) * nsp, s) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  int64_t lo = 0, mo = lists;
+  for (int k = 0; k < nsp; ++k) {
+    a[k].list       = c->gr_island + lo;
+    a[k].mask       = reinterpret_cast<unsigned*>(c->gr_island + mo);
+    a[k].list_count = c->gr_island_cnt + 2 * k;
+    lo += sp[k]->npart;
+    mo += (sp[k]->npart + 31) / 32;
+    PIC_KL(pic::k_gr_island_list<real><<<blocks_for(sp[k]->npart), 256, 0, s>>>(a[k]));
+  }
+  if (cudaEventRecord(c->gr_fork, s) != cudaSuccess) return PIC_ERR_CUDA;
+  for (int k = 0; k < nsp; ++k) {
+    cudaStream_t s2 = c->gr_side[k];
+    if (cudaStreamWaitEvent(s2, c->gr_fork, 0) != cudaSuccess) return PIC_ERR_CUDA;
+    if constexpr (sizeof(real) == 4) {
+      // three 128-thread blocks per SM fit at up to 170 registers per thread
+      const unsigned bi = 152 * 3;
+      switch (c->grid.order) {
+        case 1: PIC_KL(pic::k_gr_push_island<1, real><<<bi, 128, 0, s2>>>(a[k])); break;
+        case 2: PIC_KL(pic::k_gr_push_island<2, real><<<bi, 128, 0, s2>>>(a[k])); break;
+        default: PIC_KL(pic::k_gr_push_island<3, real><<<bi, 128, 0, s2>>>(a[k])); break;
+      }
+    }
+    if (cudaEventRecord(c->gr_join[k], s2) != cudaSuccess) return PIC_ERR_CUDA;
+  }
+  for (int k = 0; k < nsp; ++k) bulk(a[k]);
+  for (int k = 0; k < nsp; ++k)
+    if (cudaStreamWaitEvent(s, c->gr_join[k], 0) != cudaSuccess) return PIC_ERR_CUDA;
   return cuda_status(cudaGetLastError());
 }
 
@@ -835,6 +931,57 @@ int gr_deposit(pic_ctx* c, const pic_gr_metric* g, const pic_species* sp, void* 
   return cuda_status(cudaGetLastError());
 }
 
+// the species of a push that have work, after the checks of pic_gr_push
+int push_checks(pic_ctx* c, const pic_gr_metric* g, pic_species* sp, int32_t nsp,
+                const void* em, const void* em0, int32_t niter,
+                std::vector<const pic_species*>& work) {
+  int st = gr_check(c, g);
+  if (st != PIC_OK) return st;
+  if (!em || !em0 || niter < 1 || nsp < 0 || (nsp > 0 && !sp)) return PIC_ERR_ARG;
+  for (int32_t k = 0; k < nsp; ++k) {
+    st = validate_species(c, sp + k, true);
+    if (st != PIC_OK) return st;
+    if (sp[k].npart == 0 || sp[k].pusher == PIC_PUSHER_NONE) continue;
+    if (sp[k].pusher == PIC_PUSHER_VAY) return PIC_ERR_UNSUPPORTED;
+    if (sp[k].pusher == PIC_PUSHER_BORIS && sp[k].mass == 0.0f) return PIC_ERR_ARG;
+    work.push_back(sp + k);
+  }
+  return PIC_OK;
+}
+
+int push_entry(pic_ctx* c, const pic_gr_metric* g, pic_species* sp, int32_t nsp, const void* em,
+               const void* em0, double dt, double omegaB0, int32_t niter, int32_t island_lo,
+               int32_t island_hi, void* stream) {
+  std::vector<const pic_species*> work;
+  const int st = push_checks(c, g, sp, nsp, em, em0, niter, work);
+  if (st != PIC_OK || work.empty()) return st;
+  const cudaStream_t s = strm(stream);
+  const int          n = (int)work.size();
+  return is_f64(c) ? gr_push_species<double>(c, g, work.data(), n, em, em0, dt, omegaB0, niter,
+                                             island_lo, island_hi, s)
+                   : gr_push_species<float>(c, g, work.data(), n, em, em0, dt, omegaB0, niter,
+                                            island_lo, island_hi, s);
+}
+
+// the cells of the +x1 match layer (MatchFieldsIn, grpic/fields_bcs.h:53-92,
+// and Mesh::ExtentToRange, framework/domain/mesh.h:133-202): x1 over
+// [floor(x1(r_max - ds)) + ng, ceil(x1(r_max)) + 2 ng) in real_t, upper ghosts
+// included; every x2 cell, ghosts included. The end is clamped to the array.
+template <typename real>
+pic::Range2 match_range(const pic_ctx* c, const pic_gr_metric* g, double ds) {
+  const QKS<double> md = make_qks<real>(c, g);
+  const real r0 = (real)md.r0, chi_min = (real)md.chi_min, dchi_inv = (real)md.dchi_inv;
+  const real r_lo = (real)g->x1min, r_hi = (real)g->x1max;
+  const real lo   = std::min(std::max(r_lo, r_hi - (real)ds), r_hi);
+  auto       x1   = [&](real r) { return (std::log(r - r0) - chi_min) * dchi_inv; };
+  const int  ng   = c->grid.ng;
+  int        i0   = (int)std::floor(x1(lo)) + ng;
+  int        i1   = (int)std::ceil(x1(r_hi)) + 2 * ng;
+  i0 = std::max(i0, ng);
+  i1 = std::min(i1, c->grid.n[0] + 2 * ng);
+  return pic::Range2{ i0, std::max(i0, i1), 0, c->grid.n[1] + 2 * ng };
+}
+
 }  // namespace
 
 extern "C" {
@@ -854,18 +1001,14 @@ int pic_gr_metric_eval(pic_ctx* c, const pic_gr_metric* g, const double* x, int6
 int pic_gr_push(pic_ctx* c, const pic_gr_metric* g, pic_species* sp, const void* em,
                 const void* em0, double dt, double omegaB0, int32_t niter, int32_t island_lo,
                 int32_t island_hi, void* stream) {
-  int st = gr_check(c, g);
-  if (st != PIC_OK) return st;
-  if (!em || !em0 || niter < 1) return PIC_ERR_ARG;
-  st = validate_species(c, sp, true);
-  if (st != PIC_OK) return st;
-  if (sp->npart == 0 || sp->pusher == PIC_PUSHER_NONE) return PIC_OK;
-  if (sp->pusher == PIC_PUSHER_VAY) return PIC_ERR_UNSUPPORTED;
-  if (sp->pusher == PIC_PUSHER_BORIS && sp->mass == 0.0f) return PIC_ERR_ARG;
-  cudaStream_t s = strm(stream);
-  return is_f64(c)
-           ? gr_push<double>(c, g, sp, em, em0, dt, omegaB0, niter, island_lo, island_hi, s)
-           : gr_push<float>(c, g, sp, em, em0, dt, omegaB0, niter, island_lo, island_hi, s);
+  if (!sp) return PIC_ERR_ARG;
+  return push_entry(c, g, sp, 1, em, em0, dt, omegaB0, niter, island_lo, island_hi, stream);
+}
+
+int pic_gr_particle_push(pic_ctx* c, const pic_gr_metric* g, pic_species* sp, int32_t nspecies,
+                         const void* em, const void* em0, double dt, double omegaB0,
+                         int32_t niter, int32_t island_lo, int32_t island_hi, void* stream) {
+  return push_entry(c, g, sp, nspecies, em, em0, dt, omegaB0, niter, island_lo, island_hi, stream);
 }
 
 int pic_gr_deposit(pic_ctx* c, const pic_gr_metric* g, const pic_species* sp, int32_t nspecies,
@@ -1021,6 +1164,47 @@ int pic_gr_field_bcs(pic_ctx* c, const pic_gr_metric* g, void* fld, int32_t set_
     const auto f = fld_of<float>(c, g);
     if (g->axis_min || g->axis_max) PIC_KL(pic::k_gr_axis<float><<<b1, 256, 0, s>>>(f, em_view<float>(c, fld), set_e, set_b));
     if (g->horizon) PIC_KL(pic::k_gr_horizon<float><<<b2, 256, 0, s>>>(f, em_view<float>(c, fld), set_e, set_b, nfilter));
+  }
+  return cuda_status(cudaGetLastError());
+}
+
+int pic_gr_match_fields(pic_ctx* c, const pic_gr_metric* g, void* fld, const void* target,
+                        double ds, int32_t set_e, int32_t set_b, void* stream) {
+  int st = gr_check(c, g);
+  if (st != PIC_OK) return st;
+  if (!fld || !target || !(ds > 0.0)) return PIC_ERR_ARG;
+  cudaStream_t s = strm(stream);
+  if (is_f64(c)) {
+    const auto R = match_range<double>(c, g, ds);
+    if (R.count() == 0) return PIC_OK;
+    PIC_KL(pic::k_gr_match<double><<<blocks_for(R.count()), 256, 0, s>>>(
+      fld_of<double>(c, g), R, em_view<double>(c, fld), em_view<double>(c, target),
+      (double)g->x1max, ds, set_e, set_b));
+  } else {
+    const auto R = match_range<float>(c, g, ds);
+    if (R.count() == 0) return PIC_OK;
+    PIC_KL(pic::k_gr_match<float><<<blocks_for(R.count()), 256, 0, s>>>(
+      fld_of<float>(c, g), R, em_view<float>(c, fld), em_view<float>(c, target),
+      (float)g->x1max, (float)ds, set_e, set_b));
+  }
+  return cuda_status(cudaGetLastError());
+}
+
+int pic_gr_absorb_currents(pic_ctx* c, const pic_gr_metric* g, void* J, double ds, void* stream) {
+  int st = gr_check(c, g);
+  if (st != PIC_OK) return st;
+  if (!J || !(ds > 0.0)) return PIC_ERR_ARG;
+  cudaStream_t s = strm(stream);
+  if (is_f64(c)) {
+    const auto R = match_range<double>(c, g, ds);
+    if (R.count() == 0) return PIC_OK;
+    PIC_KL(pic::k_gr_absorb_currents<double><<<blocks_for(R.count()), 256, 0, s>>>(
+      fld_of<double>(c, g), R, cur_view<double>(c, J), (double)g->x1max, ds));
+  } else {
+    const auto R = match_range<float>(c, g, ds);
+    if (R.count() == 0) return PIC_OK;
+    PIC_KL(pic::k_gr_absorb_currents<float><<<blocks_for(R.count()), 256, 0, s>>>(
+      fld_of<float>(c, g), R, cur_view<float>(c, J), (float)g->x1max, (float)ds));
   }
   return cuda_status(cudaGetLastError());
 }

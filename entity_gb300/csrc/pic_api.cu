@@ -335,8 +335,8 @@ int pic_destroy(pic_ctx* c) {
   cudaFree(c->gr_island);
   cudaFree(c->gr_island_cnt);
   if (c->gr_fork) cudaEventDestroy(c->gr_fork);
-  if (c->gr_join) cudaEventDestroy(c->gr_join);
-  if (c->gr_side) cudaStreamDestroy(c->gr_side);
+  for (auto e : c->gr_join) cudaEventDestroy(e);
+  for (auto q : c->gr_side) cudaStreamDestroy(q);
   pic::adjoint_release(c->adjoint);
   delete c;
   return PIC_OK;

@@ -65,6 +65,7 @@ class GRContext(Context):
         super().__init__(g)
         self.spec = spec
         self.m = spec.metric()
+        self.match = None
 
     def metric_eval(self, x, stream=None):
         x = torch.as_tensor(x, dtype=torch.float64, device="cuda").contiguous()
@@ -79,6 +80,13 @@ class GRContext(Context):
         ps = make_species(sp, 2)
         abi.call("pic_gr_push", self.h, C.byref(self.m), C.byref(ps), _ptr(em), _ptr(em0), dt,
                  omegaB0, niter, island[0], island[1], _stream_ptr(stream))
+
+    def gr_particle_push(self, species, em, em0, dt, omegaB0, niter=10, island=(0, 0),
+                         stream=None):
+        """grpic::ParticlePush: every species, islands run concurrently."""
+        arr = (abi.PicSpecies * len(species))(*[make_species(s, 2) for s in species])
+        abi.call("pic_gr_particle_push", self.h, C.byref(self.m), arr, len(species), _ptr(em),
+                 _ptr(em0), dt, omegaB0, niter, island[0], island[1], _stream_ptr(stream))
 
     def gr_deposit(self, species, J, dt, island=(0, 0), zero=True, stream=None):
         arr = (abi.PicSpecies * len(species))(*[make_species(s, 2) for s in species])
@@ -128,13 +136,25 @@ class GRContext(Context):
                  _stream_ptr(stream))
         return out.value
 
-    def grpic_step(self, species, fields, prm, niter=10, island=(0, 0), step=0, stream=None):
+    def gr_match_fields(self, fld, target, ds, set_e=True, set_b=True, stream=None):
+        abi.call("pic_gr_match_fields", self.h, C.byref(self.m), _ptr(fld), _ptr(target), ds,
+                 int(set_e), int(set_b), _stream_ptr(stream))
+
+    def gr_absorb_currents(self, J, ds, stream=None):
+        abi.call("pic_gr_absorb_currents", self.h, C.byref(self.m), _ptr(J), ds,
+                 _stream_ptr(stream))
+
+    def grpic_step(self, species, fields, prm, niter=10, island=(0, 0), step=0, match=None,
+                   stream=None):
         """fields: list [em, em0, aux, cur, cur0, buff]; swapped in place like
-        the reference's views."""
+        the reference's views. match = (ds, target field) enables the MATCH
+        boundary at r max."""
         arr = (abi.PicSpecies * len(species))(*[make_species(s, 2) for s in species])
         ptrs = (C.c_void_p * 6)(*[t.data_ptr() for t in fields])
         gp = abi.PicGRParams()
         gp.niter, gp.island_lo, gp.island_hi = niter, island[0], island[1]
+        if match is not None:
+            gp.match_ds, gp.match_target = float(match[0]), match[1].data_ptr()
         abi.call("pic_grpic_step", self.h, C.byref(self.m), arr, len(species), ptrs,
                  C.byref(prm), C.byref(gp), step, _stream_ptr(stream))
         by_ptr = {t.data_ptr(): t for t in fields}
@@ -205,7 +225,8 @@ def wald_setup(n=(1024, 512), a=0.95, r_max=50.0, order=2, ppc=4, r_inject=6.0,
     device by pic_gr_inject_uniform_maxwellians: `ppc` pairs per cell on
     average, uniform in code coordinates over r < r_inject, weights
     sqrt(det h) / V0 (the reference's GR injection weights), V0 = sqrt(det h)
-    at the first cell centre; then one cell sort of each species."""
+    at the first cell centre; then one cell sort of each species. ctx.match
+    holds the MATCH boundary's (ds, target field) for grpic_step."""
     from .inputs import empty_species, inject_params
     g = gr_grid(n[0], n[1], order=order, real=real)
     spec = GRSpec(a=a, r_max=r_max)
@@ -214,6 +235,10 @@ def wald_setup(n=(1024, 512), a=0.95, r_max=50.0, order=2, ppc=4, r_inject=6.0,
     ctx.gr_init_vertical(em)
     fields = [em, torch.zeros_like(em), torch.zeros_like(em), empty_field(g, 3, "cuda"),
               empty_field(g, 3, "cuda"), empty_field(g, 3, "cuda")]
+    # MATCH at r max toward the seed field, ds = 1 % of the radial extent
+    # (grid.boundaries.match.ds's default, parameters/grid.cpp:295-305)
+    m = spec.metric()
+    ctx.match = (0.01 * (m.x1max - m.x1min), em.clone())
     x1_inj = min(float(g.n[0]), spec.x1_of_r(g, r_inject))
     cap = int(math.ceil(ppc * x1_inj * g.n[1])) + 1
     species = [empty_species(g, cap, charge=q, index=k + 1) for k, q in enumerate((-1.0, 1.0))]

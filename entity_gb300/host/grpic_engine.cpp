@@ -1,9 +1,9 @@
 // GRPICEngine::step_forward (src/engines/grpic/grpic.hpp:66-634) over the C
 // ABI: the leapfrog of D, B (em at the newer time, em0 at the older one),
 // the auxiliary E and H, the GR push and deposit, and the field swap, with
-// the axis and horizon field boundaries. CommunicateFields and
-// SynchronizeFields are no-ops on one non-periodic (r, theta) domain; the
-// MATCH boundary at large r and the current filter are not applied.
+// the axis, horizon and (optionally) MATCH field boundaries and the current
+// absorption at r max. CommunicateFields and SynchronizeFields are no-ops on
+// one non-periodic (r, theta) domain; the current filter is not applied.
 #include <cstdint>
 #include <cuda_runtime.h>
 #include <utility>
@@ -23,10 +23,18 @@ int gr_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, int32_t nsp, 
     return st;
   auto mark = [&](int phase, int end) { return pic_timer_mark(ctx, phase, end, stream); };
   // gr_bc::main boundaries act on both em and em0 (grpic/fields_bcs.h:220-262)
-  auto bc_main = [&](int set_e, int set_b) {
-    int s = pic_gr_field_bcs(ctx, m, f[0], set_e, set_b, p.nfilter, stream);
-    if (s != PIC_OK) return s;
-    return pic_gr_field_bcs(ctx, m, f[1], set_e, set_b, p.nfilter, stream);
+  // the directions in Directions<2>::orth order: horizon (-x1), axis (-x2,
+  // +x2), match (+x1)
+  const bool match  = gp.match_ds > 0.0;
+  auto       bc_main = [&](int set_e, int set_b) {
+    for (int k = 0; k < 2; ++k) {
+      int s = pic_gr_field_bcs(ctx, m, f[k], set_e, set_b, p.nfilter, stream);
+      if (s == PIC_OK && match)
+        s = pic_gr_match_fields(ctx, m, f[k], gp.match_target, gp.match_ds, set_e, set_b,
+                                stream);
+      if (s != PIC_OK) return s;
+    }
+    return (int)PIC_OK;
   };
   auto swap = [&]() {
     std::swap(f[0], f[1]);
@@ -38,6 +46,9 @@ int gr_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, int32_t nsp, 
   const real dThalf = (real)0.5 * (real)p.correction * dt;
   const real jcoeff = -dt * (real)p.q0 / (real)p.B0;
   const bool fs = p.fieldsolver_enabled != 0, dep = p.deposit_enabled != 0;
+  pic_grid   g;
+  PIC_TRY(pic_get_grid(ctx, &g));
+  const bool absorb_max = g.prtl_bc[0][1] == PIC_BC_ABSORB;
   void*      aux = f[2];
 
   PIC_TRY(mark(PIC_PHASE_STEP, 0));
@@ -81,14 +92,14 @@ int gr_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, int32_t nsp, 
     PIC_TRY(mark(PIC_PHASE_FIELDSOLVER, 1));
   }
   PIC_TRY(mark(PIC_PHASE_PUSH_DEPOSIT, 0));
-  for (int32_t k = 0; k < nsp; ++k) {
-    if (sp[k].npart == 0 || sp[k].pusher == PIC_PUSHER_NONE) continue;
-    PIC_TRY(pic_gr_push(ctx, m, sp + k, f[0], f[1], (double)dt, (double)(real)p.omegaB0,
-                        gp.niter, gp.island_lo, gp.island_hi, stream));
-  }
-  if (dep)
+  PIC_TRY(pic_gr_particle_push(ctx, m, sp, nsp, f[0], f[1], (double)dt, (double)(real)p.omegaB0,
+                               gp.niter, gp.island_lo, gp.island_hi, stream));
+  if (dep) {
     PIC_TRY(pic_gr_deposit(ctx, m, sp, nsp, f[4], (double)dt, gp.island_lo, gp.island_hi, 0u,
                            stream));
+    // FieldBoundaries(gr_bc::curr): absorbing particles at r max (fields_bcs.h:262-268)
+    if (match && absorb_max) PIC_TRY(pic_gr_absorb_currents(ctx, m, f[4], gp.match_ds, stream));
+  }
   PIC_TRY(mark(PIC_PHASE_PUSH_DEPOSIT, 1));
   if (fs) {
     PIC_TRY(mark(PIC_PHASE_FIELDSOLVER, 0));
@@ -129,6 +140,7 @@ extern "C" int pic_grpic_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species*
   for (int k = 0; k < 5; ++k)
     if (!fields[k]) return PIC_ERR_ARG;
   if (prm->nfilter != 0 || gprm->niter < 1) return PIC_ERR_UNSUPPORTED;
+  if (gprm->match_ds < 0.0 || (gprm->match_ds > 0.0 && !gprm->match_target)) return PIC_ERR_ARG;
   pic_grid g;
   int      st = pic_get_grid(ctx, &g);
   if (st != PIC_OK) return st;

@@ -412,6 +412,15 @@ int pic_gr_push(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, const voi
                 const void* em0, double dt, double omegaB0, int32_t niter, int32_t island_lo,
                 int32_t island_hi, void* stream);
 
+/* grpic::ParticlePush (src/engines/grpic/particle_pusher.h:26-94): the push
+ * of pic_gr_push for every species with particles and a pusher. The FP64
+ * islands of all species run at once, each on its own stream beside the
+ * single-precision bulk. */
+int pic_gr_particle_push(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp,
+                         int32_t nspecies, const void* em, const void* em0, double dt,
+                         double omegaB0, int32_t niter, int32_t island_lo, int32_t island_hi,
+                         void* stream);
+
 /* grpic::CurrentsDeposit (src/engines/grpic/currents.h:29-73): the current
  * of the last push at shape order 1 (hard-wired in the reference) with the
  * metric out-of-plane velocity (currents_deposit.hpp:138-159), evaluated
@@ -450,6 +459,20 @@ int pic_gr_average(pic_ctx* ctx, int32_t which, void* a, void* b, void* stream);
  * the D (E) and B (H) components */
 int pic_gr_field_bcs(pic_ctx* ctx, const pic_gr_metric* m, void* fld, int32_t set_e,
                      int32_t set_b, int32_t nfilter, void* stream);
+/* MatchFieldsIn at +x1 (src/engines/grpic/fields_bcs.h:42-137) with
+ * MatchBoundaries_kernel's GRPIC branch (src/kernels/fields_bcs.hpp:181-340):
+ * over the cells of the layer r in [r_max - ds, r_max] (upper ghosts and all
+ * theta cells included), each component relaxes toward `target`:
+ * F = s F + (1 - s) target, s = tanh(4 |r - r_max| / ds) at the component's
+ * radius. The reference evaluates the problem generator's field setter
+ * there; the caller stores that field in `target` (em layout). set_e / set_b
+ * select the D and B components. */
+int pic_gr_match_fields(pic_ctx* ctx, const pic_gr_metric* m, void* fld, const void* target,
+                        double ds, int32_t set_e, int32_t set_b, void* stream);
+/* gr::AbsorbCurrents_kernel (src/kernels/fields_bcs.hpp:1243-1280) over the
+ * same layer: J *= tanh(|r - r_max| / (ds / 4)) at the cell's radius. */
+int pic_gr_absorb_currents(pic_ctx* ctx, const pic_gr_metric* m, void* J, double ds,
+                           void* stream);
 /* the vertical seed field of pgens/wald (InitFields, init_field = vertical)
  * on every cell, ghosts included; D = 0 */
 int pic_gr_init_vertical(pic_ctx* ctx, const pic_gr_metric* m, void* EB, void* stream);
@@ -459,17 +482,21 @@ int pic_gr_min_cell_size(pic_ctx* ctx, const pic_gr_metric* m, double* out, void
 
 /* GR step parameters beyond pic_step_params */
 typedef struct {
-  int32_t niter;      /* pusher iterations (algorithms.gr.pusher_niter, default 10) */
-  int32_t island_lo;  /* particles with island_lo <= i1 < island_hi run the */
-  int32_t island_hi;  /* pusher in FP64 (single-precision builds) */
+  int32_t     niter;        /* pusher iterations (algorithms.gr.pusher_niter, default 10) */
+  int32_t     island_lo;    /* particles with island_lo <= i1 < island_hi run the */
+  int32_t     island_hi;    /* pusher in FP64 (single-precision builds) */
+  double      match_ds;     /* > 0: MATCH fields at r max (grid.boundaries.match.ds) */
+  const void* match_target; /* the field MATCH relaxes toward (6 components, em layout) */
 } pic_gr_params;
 
 /* GRPICEngine::step_forward (src/engines/grpic/grpic.hpp:66-634) on one
  * domain: fields[0..5] = em, em0, aux, cur, cur0, buff (device pointers);
  * the step swaps em <-> em0 and cur <-> cur0 in the array as the reference
  * swaps its views. Step 0 runs the reference's initialisation block.
- * Filters are not supported (nfilter must be 0); MATCH field boundaries are
- * not applied (ghost cells at r max keep their values). */
+ * Filters are not supported (nfilter must be 0). With gprm->match_ds > 0
+ * the MATCH boundary at r max follows the axis and horizon boundaries on em
+ * and em0 (FieldBoundaries, gr_bc::main), and, when particles are absorbed
+ * at r max, the currents are absorbed there after the deposit (gr_bc::curr). */
 int pic_grpic_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, int32_t nspecies,
                    void* fields[6], const pic_step_params* prm, const pic_gr_params* gprm,
                    int64_t step, void* stream);

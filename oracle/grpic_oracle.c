@@ -543,6 +543,90 @@ void orc_gr_field_bcs(const orc_grid* g, void* fld_, int set_e, int set_b, int a
   }
 }
 
+/* the +x1 match layer's cells (MatchFieldsIn, grpic/fields_bcs.h:53-92, and
+ * Mesh::ExtentToRange, mesh.h:133-202), x1 end clamped to the array */
+static void match_range(const orc_grid* g, const orc_qks* q, double ds, double r_lo, double r_hi,
+                        int* i0, int* i1) {
+  const real r0 = (real)q->r0, chi_min = (real)q->chi_min, dchi_inv = (real)q->dchi_inv;
+  const real hi = (real)r_hi, lo_raw = (real)r_hi - (real)ds;
+  const real lo = lo_raw < (real)r_lo ? (real)r_lo : (lo_raw > hi ? hi : lo_raw);
+#ifdef ORC_SINGLE
+  const real xlo = (logf(lo - r0) - chi_min) * dchi_inv, xhi = (logf(hi - r0) - chi_min) * dchi_inv;
+  int        a = (int)floorf(xlo) + g->ng, b = (int)ceilf(xhi) + 2 * g->ng;
+#else
+  const real xlo = (log(lo - r0) - chi_min) * dchi_inv, xhi = (log(hi - r0) - chi_min) * dchi_inv;
+  int        a = (int)floor(xlo) + g->ng, b = (int)ceil(xhi) + 2 * g->ng;
+#endif
+  if (a < g->ng) a = g->ng;
+  if (b > g->n1 + 2 * g->ng) b = g->n1 + 2 * g->ng;
+  *i0 = a;
+  *i1 = b < a ? a : b;
+}
+
+/* the radius at code coordinate x1 (QKerrSchild::convert<1, Cd, Ph>) */
+static real r_of(const orc_qks* q, real x1) {
+#ifdef ORC_SINGLE
+  return (real)q->r0 + expf(x1 * (real)q->dchi + (real)q->chi_min);
+#else
+  return (real)q->r0 + exp(x1 * (real)q->dchi + (real)q->chi_min);
+#endif
+}
+
+/* MatchBoundaries_kernel, GRPIC branch, 2D, o = x1 (fields_bcs.hpp:181-340) */
+void orc_gr_match(const orc_grid* g, const orc_qks* q, void* fld_, const void* tgt_, double ds,
+                  double r_lo, double r_hi, int set_e, int set_b, int axis_min, int axis_max) {
+  real*       F = (real*)fld_;
+  const real* T = (const real*)tgt_;
+  int         i0, i1e;
+  match_range(g, q, ds, r_lo, r_hi, &i0, &i1e);
+  const real H = 0.5, ONE = 1, FOUR = 4, edge = (real)r_hi, dsr = (real)ds;
+  const int  N2 = g->n2 + 2 * g->ng;
+  for (int i1 = i0; i1 < i1e; ++i1) {
+    const real i1_ = (real)(i1 - g->ng);
+#ifdef ORC_SINGLE
+    const real sH = tanhf(fabsf(r_of(q, i1_ + H) - edge) * FOUR / dsr);
+    const real s0 = tanhf(fabsf(r_of(q, i1_) - edge) * FOUR / dsr);
+#else
+    const real sH = tanh(fabs(r_of(q, i1_ + H) - edge) * FOUR / dsr);
+    const real s0 = tanh(fabs(r_of(q, i1_) - edge) * FOUR / dsr);
+#endif
+    for (int i2 = 0; i2 < N2; ++i2) {
+      if (set_e) {
+        F[EBI(g, i1, i2, 0)] = sH * F[EBI(g, i1, i2, 0)] + (ONE - sH) * T[EBI(g, i1, i2, 0)];
+        F[EBI(g, i1, i2, 1)] = s0 * F[EBI(g, i1, i2, 1)] + (ONE - s0) * T[EBI(g, i1, i2, 1)];
+        F[EBI(g, i1, i2, 2)] = s0 * F[EBI(g, i1, i2, 2)];
+        if ((!axis_min || i2 > g->ng) && (!axis_max || i2 < N2 - g->ng))
+          F[EBI(g, i1, i2, 2)] += (ONE - s0) * T[EBI(g, i1, i2, 2)];
+      }
+      if (set_b) {
+        F[EBI(g, i1, i2, 3)] = s0 * F[EBI(g, i1, i2, 3)] + (ONE - s0) * T[EBI(g, i1, i2, 3)];
+        F[EBI(g, i1, i2, 4)] = sH * F[EBI(g, i1, i2, 4)] + (ONE - sH) * T[EBI(g, i1, i2, 4)];
+        F[EBI(g, i1, i2, 5)] = sH * F[EBI(g, i1, i2, 5)] + (ONE - sH) * T[EBI(g, i1, i2, 5)];
+      }
+    }
+  }
+}
+
+/* gr::AbsorbCurrents_kernel<M, 1> (fields_bcs.hpp:1243-1280) */
+void orc_gr_absorb_currents(const orc_grid* g, const orc_qks* q, void* J_, double ds,
+                            double r_lo, double r_hi) {
+  real* J = (real*)J_;
+  int   i0, i1e;
+  match_range(g, q, ds, r_lo, r_hi, &i0, &i1e);
+  const real INV_4 = 0.25, edge = (real)r_hi, dsr = (real)ds;
+  const int  N2 = g->n2 + 2 * g->ng;
+  for (int i1 = i0; i1 < i1e; ++i1) {
+    const real i1_ = (real)(i1 - g->ng);
+#ifdef ORC_SINGLE
+    const real t = tanhf(fabsf(r_of(q, i1_) - edge) / (INV_4 * dsr));
+#else
+    const real t = tanh(fabs(r_of(q, i1_) - edge) / (INV_4 * dsr));
+#endif
+    for (int i2 = 0; i2 < N2; ++i2)
+      for (int c = 0; c < 3; ++c) J[JI(g, i1, i2, c)] *= t;
+  }
+}
+
 /* the GRPIC branch of UniformInjector_kernel (injectors.hpp:230-239): the
  * tetrad-frame sample transformed to covariant components at the particle
  * (transform<Idx::T, Idx::D>), weight sqrt(det h) / V0 there */

@@ -90,6 +90,13 @@ void orc_gr_average_j(const orc_grid* g, void* J, const void* J0);
 void orc_gr_field_bcs(const orc_grid* g, void* fld, int set_e, int set_b, int axis_min,
                       int axis_max, int horizon, int nfilter);
 
+/* MATCH at +x1 toward `target` over r in [r_hi - ds, r_hi] (r_lo, r_hi: the
+ * grid's radial extent), and the current absorption over the same layer */
+void orc_gr_match(const orc_grid* g, const orc_qks* q, void* fld, const void* target, double ds,
+                  double r_lo, double r_hi, int set_e, int set_b, int axis_min, int axis_max);
+void orc_gr_absorb_currents(const orc_grid* g, const orc_qks* q, void* J, double ds, double r_lo,
+                            double r_hi);
+
 /* the uniform Maxwellian pair injection on the QKerrSchild grid
  * (inject_oracle.h for the random numbers): covariant velocities, weight
  * sqrt(det h) / V0 */

@@ -307,6 +307,8 @@ def _gr_sigs(L):
     L.orc_gr_average_db.argtypes = [G, V, V]
     L.orc_gr_average_j.argtypes = [G, V, V]
     L.orc_gr_field_bcs.argtypes = [G, V, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.orc_gr_match.argtypes = [G, Q, V, V, D, D, D, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.orc_gr_absorb_currents.argtypes = [G, Q, V, D, D, D]
     L.orc_gr_inject_uniform.restype = C.c_int64
     L.orc_gr_inject_uniform.argtypes = [G, Q, S, S, C.POINTER(OrcInjectParams), D,
                                         C.POINTER(C.c_int64)]
@@ -323,6 +325,15 @@ class GROracle(Oracle):
         self.q = OrcQKS()
         self.L.orc_qks_init(C.byref(self.q), g.n[0], g.n[1], r_min, r_max, th_min, th_max, a,
                             r0, h)
+        self.r_min, self.r_max = r_min, r_max
+
+    def gr_match(self, fld, target, ds, set_e=1, set_b=1, axis_min=1, axis_max=1):
+        self.L.orc_gr_match(C.byref(self.og), C.byref(self.q), _p(fld), _p(target), ds,
+                            self.r_min, self.r_max, int(set_e), int(set_b), axis_min, axis_max)
+
+    def gr_absorb_currents(self, J, ds):
+        self.L.orc_gr_absorb_currents(C.byref(self.og), C.byref(self.q), _p(J), ds, self.r_min,
+                                      self.r_max)
 
     def gr_inject_uniform(self, sp1, sp2, params, V0):
         s1, s2 = self.species(sp1), self.species(sp2)
@@ -392,14 +403,18 @@ class GROracle(Oracle):
     # GRPICEngine::step_forward (grpic.hpp:66-634), the sequence of the
     # product's engine: fields = [em, em0, aux, cur, cur0, buff], swapped in
     # place; axis/horizon boundaries on em and em0 after each update
-    def grpic_step(self, species, fields, prm, niter=10, island=(0, 0), step=0, flags=(1, 1, 1)):
+    def grpic_step(self, species, fields, prm, niter=10, island=(0, 0), step=0, flags=(1, 1, 1),
+                   match=None):
         R = self.g.real
         t = lambda v: torch.tensor(v, dtype=R)
         amin, amax, hor = flags
 
         def bc(set_e, set_b):
+            # orth order: horizon (-x1), axis (-x2, +x2), match (+x1)
             for f in fields[:2]:
                 self.gr_field_bcs(f, set_e, set_b, amin, amax, hor, prm.nfilter)
+                if match is not None:
+                    self.gr_match(f, match[1], match[0], set_e, set_b, amin, amax)
 
         def swap():
             fields[0], fields[1] = fields[1], fields[0]
@@ -446,6 +461,8 @@ class GROracle(Oracle):
                 self.gr_push(sp, em, em0, float(dt), prm.omegaB0, niter, island=island)
         if dep:
             self.gr_deposit(species, fields[4], float(dt), island=island)
+            if match is not None and self.g.prtl_bc[0][1] == 1:
+                self.gr_absorb_currents(fields[4], match[0])
         if fs:
             cur, cur0 = fields[3], fields[4]
             if dep:

@@ -108,6 +108,34 @@ def test_gr_push_matches_oracle(real, order, pusher):
         assert float((a - b)[alive].abs().max()) <= tol * 10 * scale, c
 
 
+@pytest.mark.parametrize("real", REALS)
+def test_gr_particle_push_all_species(real):
+    """pic_gr_particle_push over three species (electrons, positrons,
+    photons; the islands run on their own streams) against the oracle's
+    push of each species."""
+    g, spec, ctx, o = _setup(real, order=2)
+    em, em0 = _rand_fields(g, 1), _rand_fields(g, 2)
+    sps = [_particles(g, 3000, 21, charge=-1.0), _particles(g, 2500, 22, charge=1.0),
+           _particles(g, 2000, 23, pusher=3)]
+    island = (g.n[0] // 6, g.n[0] // 3)
+    gpu = [s.clone().to("cuda") for s in sps]
+    for s in sps:
+        o.gr_push(s, em, em0, 0.05, 2.0, 10, island=island)
+    ctx.gr_particle_push(gpu, em.cuda(), em0.cuda(), 0.05, 2.0, 10, island=island)
+    torch.cuda.synchronize()
+    assert ctx.device_errors() == [0, 0, 0, 0]
+    tol = TOL[real]
+    for s, sg in zip(sps, gpu):
+        assert torch.equal(s.tag, sg.tag.cpu())
+        alive = s.tag == 1
+        for d in range(2):
+            assert float((_X(s, d) - _X(sg, d))[alive].abs().max()) <= tol * 50
+        for c in range(3):
+            a, b = s.u[c].double(), sg.u[c].cpu().double()
+            scale = float(a.abs().max()) + 1e-30
+            assert float((a - b)[alive].abs().max()) <= tol * 10 * scale, c
+
+
 @pytest.mark.parametrize("band", [(0, 48), (8, 9), (30, 10)])
 def test_gr_push_island_bands(band):
     """FP32 with the island band covering every cell (many more 32-particle
@@ -288,3 +316,69 @@ def test_gr_magnetic_flux_stays_divergence_free(real):
         ctx.grpic_step(species, fields, prm, niter=10, island=island, step=step)
     d1, s1 = div(fields[0])
     assert float(d1.abs().max()) <= 20 * eps * s1
+
+
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("tags", [(1, 1), (1, 0), (0, 1)])
+def test_gr_match_matches_oracle(real, tags):
+    """MatchBoundaries_kernel (GRPIC, +r) toward a target field, both axes on."""
+    g, spec, ctx, o = _setup(real, order=2, n=(48, 32), r_max=20.0)
+    F, T = _rand_fields(g, 3), _rand_fields(g, 4)
+    ds = 4.0
+    Fg = F.cuda()
+    o.gr_match(F, T, ds, *tags)
+    ctx.gr_match_fields(Fg, T.cuda(), ds, *tags)
+    torch.cuda.synchronize()
+    Fc = Fg.cpu()
+    scale = float(F.abs().max())
+    assert float((F.double() - Fc.double()).abs().max()) <= TOL[real] * scale
+    # below the layer nothing changes, bit for bit
+    ng = g.ng
+    assert torch.equal(F[:, 0, :, :20 + ng], Fc[:, 0, :, :20 + ng])
+
+
+@pytest.mark.parametrize("real", REALS)
+def test_gr_absorb_currents_matches_oracle(real):
+    from entity_gb300.inputs import empty_field
+    g, spec, ctx, o = _setup(real, order=2, n=(48, 32), r_max=20.0)
+    J = _rand_fields(g, 6)[:3].clone()
+    Jg = J.cuda()
+    o.gr_absorb_currents(J, 4.0)
+    ctx.gr_absorb_currents(Jg, 4.0)
+    torch.cuda.synchronize()
+    scale = float(J.abs().max())
+    assert float((J.double() - Jg.cpu().double()).abs().max()) <= TOL[real] * scale
+
+
+@pytest.mark.parametrize("real", REALS)
+def test_grpic_step_with_match_matches_oracle(real):
+    """Five GR steps with the MATCH boundary at r max relaxing toward the
+    initial vertical field and the currents absorbed there."""
+    from entity_gb300.gr import gr_step_params, horizon_island, inject_pairs
+    from entity_gb300.inputs import empty_field
+    g, spec, ctx, o = _setup(real, order=2, n=(64, 48), r_max=15.0)
+    em = empty_field(g, 6, "cuda")
+    ctx.gr_init_vertical(em)
+    target = em.clone()
+    fields = [em, torch.zeros_like(em), torch.zeros_like(em), empty_field(g, 3, "cuda"),
+              empty_field(g, 3, "cuda"), empty_field(g, 3, "cuda")]
+    # pairs out to r = 14 so that the layer holds current
+    species = inject_pairs(g, spec, 2, 14.0, 3)
+    prm = gr_step_params(ctx, cfl=0.5, ppc0=2.0, skindepth0=0.5, larmor0=0.25)
+    island = horizon_island(g, spec)
+    ds = 1.5
+    cpu_fields = [f.cpu().clone() for f in fields]
+    cpu_species = [s.clone().to("cpu") for s in species]
+    tgt_cpu = target.cpu()
+    for step in range(5):
+        ctx.grpic_step(species, fields, prm, niter=10, island=island, step=step,
+                       match=(ds, target))
+        o.grpic_step(cpu_species, cpu_fields, prm, niter=10, island=island, step=step,
+                     match=(ds, tgt_cpu))
+    torch.cuda.synchronize()
+    assert ctx.device_errors() == [0, 0, 0, 0]
+    tol = 2e-3 if real == torch.float32 else 1e-9
+    for k, name in ((0, "em"), (1, "em0"), (3, "cur")):
+        a, b = cpu_fields[k].double(), fields[k].cpu().double()
+        scale = float(a.abs().max()) + 1e-30
+        assert float((a - b).abs().max()) <= tol * scale, name

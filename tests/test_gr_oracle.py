@@ -159,3 +159,55 @@ def test_geodesic_push_conserves_killing_energy_and_angular_momentum():
     # the half E pushes round-trip u through the tetrad basis: exact up to rounding
     assert torch.allclose(sp.u[2], u3, rtol=1e-12, atol=1e-12)
     assert float(((energy() - E0) / E0).abs().max()) < 1e-3
+
+
+@pytest.mark.parametrize("real", REALS)
+def test_match_layer_relaxes_to_the_target(real):
+    """MatchBoundaries_kernel (fields_bcs.hpp:181-340): s = tanh(4 |r - r_max|
+    / ds) is 0 at r_max and ~1 a layer-width inside, so a field equal to the
+    target plus a perturbation keeps the perturbation in the interior, loses
+    it at the edge, and equals the target after repeated application
+    wherever s < 1; cells below the layer are never touched."""
+    from entity_gb300.inputs import empty_field
+    o, g = _qks(real, n=(64, 16), a=0.9, r0=0.0, rmin=1.2, rmax=20.0)
+    ds = 3.0
+    T = empty_field(g, 6)
+    gen = torch.Generator().manual_seed(5)
+    T.copy_(torch.rand(T.shape, generator=gen, dtype=torch.float64).to(real))
+    F0 = T + 0.5
+    F = F0.clone()
+    o.gr_match(F, T, ds, 1, 1, axis_min=0, axis_max=0)
+    ng = g.ng
+    # the layer's first cell: floor(x1(r_max - ds)) (ExtentToRange)
+    chi = lambda r: math.log(r)
+    x1 = lambda r: (chi(r) - chi(1.2)) / ((chi(20.0) - chi(1.2)) / 64)
+    i0 = int(math.floor(x1(20.0 - ds))) + ng
+    assert torch.equal(F[:, 0, :, :i0], F0[:, 0, :, :i0])
+    dev = (F - T)[:, 0, :, i0:].abs()
+    assert float(dev.max()) <= 0.5 + 1e-6
+    # at r_max (i1 = n1 + ng, x1 = n1) the components at integer x1 match exactly
+    edge = (F - T)[[1, 2, 3], 0, :, 64 + ng].abs()
+    assert float(edge.max()) <= 1e-5
+    for _ in range(400):
+        o.gr_match(F, T, ds, 1, 1, axis_min=0, axis_max=0)
+    # within a cell of the edge s <= tanh(4 dr / ds) ~ 0.83: the perturbation
+    # is gone after 400 passes; deeper in, less of it is removed
+    assert float((F - T)[:, 0, :, 64 + ng - 1:].abs().max()) <= 1e-4
+    depth = (F - T)[3, 0, 4, i0:64 + ng].abs().double()
+    assert torch.all(depth[1:] <= depth[:-1] + 1e-6)
+
+
+@pytest.mark.parametrize("real", REALS)
+def test_absorb_currents_layer(real):
+    """AbsorbCurrents_kernel: J *= tanh(|r - r_max| / (ds / 4)); zero at
+    r_max, untouched below the layer."""
+    from entity_gb300.inputs import empty_field
+    o, g = _qks(real, n=(64, 16), a=0.9, r0=0.0, rmin=1.2, rmax=20.0)
+    J = empty_field(g, 3)
+    J.fill_(1.0)
+    o.gr_absorb_currents(J, 3.0)
+    ng = g.ng
+    assert float(J[:, 0, :, 64 + ng].abs().max()) <= 1e-5
+    assert torch.all(J[:, 0, :, :40] == 1.0)
+    prof = J[0, 0, 5, 40:64 + ng + 1].double()
+    assert torch.all(prof[1:] <= prof[:-1] + 1e-7)   # decays toward r_max
