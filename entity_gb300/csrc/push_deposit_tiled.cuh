@@ -74,10 +74,10 @@ struct FixedAcc<float> {
     atomicAdd(w + plane, __float_as_uint(t) - MBITS);
   }
   __device__ static bool nonzero(const unsigned* w, int plane) { return (w[0] | w[plane]) != 0u; }
-  __device__ static float value(const unsigned* w, int plane, float unscale) {
-    const long long t = (long long)(int)w[plane] * 4096 + (long long)(int)w[0];
-    return __ll2float_rn(t) * unscale;
+  __device__ static long long total(const unsigned* w, int plane) {
+    return (long long)(int)w[plane] * 4096 + (long long)(int)w[0];
   }
+  __device__ static float to_real(long long t, float unscale) { return __ll2float_rn(t) * unscale; }
 };
 template <>
 struct FixedAcc<double> {
@@ -95,11 +95,14 @@ struct FixedAcc<double> {
   __device__ static bool nonzero(const unsigned* w, int plane) {
     return (w[0] | w[plane] | w[2 * plane] | w[3 * plane]) != 0u;
   }
-  __device__ static double value(const unsigned* w, int plane, double unscale) {
+  __device__ static long long total(const unsigned* w, int plane) {
     const unsigned long long t = ((unsigned long long)(long long)(int)w[3 * plane] << 48) +
                                  ((unsigned long long)w[2 * plane] << 32) +
                                  ((unsigned long long)w[plane] << 16) + w[0];
-    return __ll2double_rn((long long)t) * unscale;
+    return (long long)t;
+  }
+  __device__ static double to_real(long long t, double unscale) {
+    return __ll2double_rn(t) * unscale;
   }
 };
 
@@ -109,9 +112,14 @@ template <int D, typename real, int O>
 struct TileShape {
   static constexpr int X = 32, Y = 32, Z = 1, NT = 256;  // 2D
 };
+// 3D FP32 at order 3: 8^3 cells, so that two copies of the J window fit
+// (measured on the 96^3 sweep plasma, 2 x 32 ppc: 28.1 ms per step against
+// 34.7 ms with one copy and 16 x 8 x 4 tiles). At order 2 the copies did not
+// pay (50.5 against 48.1 ms on the 256^3 turbulence plasma, 2 x 8 ppc): its
+// warps span several cells, so fewer lanes share a word.
 template <int O>
 struct TileShape<3, float, O> {
-  static constexpr int X = 16, Y = 8, Z = (O == 3 ? 4 : 8), NT = 512;
+  static constexpr int X = (O == 3 ? 8 : 16), Y = 8, Z = 8, NT = 512;
 };
 template <int O>
 struct TileShape<3, double, O> {
@@ -166,11 +174,17 @@ struct TiledGeom {
   static constexpr int WJ2 = D == 3 ? TZ + H::J_LO + H::J_HI : 1;
   static constexpr int NE  = WE0 * WE1 * WE2;
   static constexpr int NJ  = WJ0 * WJ1 * WJ2;
-  // J window: FixedAcc<real>::WORDS planes of 3 * NJ 32-bit words
+  // J window: FixedAcc<real>::WORDS planes of 3 * NJ 32-bit words, in COPIES
+  // copies (3D FP32 at order 3: two, one per lane parity) COPY words apart
   static constexpr int    WORDS      = FixedAcc<real>::WORDS;
   static constexpr int    PLANE      = 3 * NJ;
+  static constexpr int    COPIES     = (D == 3 && sizeof(real) == 4 && O == 3) ? 2 : 1;
+  // the copies start 16 banks apart: one word in both copies falls in
+  // two different banks
+  static constexpr int    COPY       = WORDS * PLANE + ((16 - (WORDS * PLANE) % 32) + 32) % 32;
   static constexpr size_t eb_bytes   = sizeof(real) * 6 * (size_t)NE;
-  static constexpr size_t smem_bytes = ((eb_bytes + 15) / 16) * 16 + 4 * (size_t)WORDS * PLANE;
+  static constexpr size_t smem_bytes = ((eb_bytes + 15) / 16) * 16 +
+                                       4 * (size_t)(COPIES == 1 ? WORDS * PLANE : COPIES * COPY);
 };
 
 // wraps a ghost-free coordinate of a periodic axis into [0, n)
@@ -223,7 +237,9 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
     }
     EBs[idx] = inside ? a.EB.ld(gc[0] + ng, gc[1] + ng, D == 3 ? gc[2] + ng : 0, c) : (real)0;
   }
-  for (int idx = threadIdx.x; idx < G::WORDS * G::PLANE; idx += NT) Jw[idx] = 0u;
+  for (int idx = threadIdx.x; idx < (G::COPIES == 1 ? G::WORDS * G::PLANE : G::COPIES * G::COPY);
+       idx += NT)
+    Jw[idx] = 0u;
   // largest contribution bound of the tile, |q w| max(1/dt, 1), and its
   // particle count (an upper bound on the additions any cell receives)
   if (threadIdx.x == 0) s_qmax = 0u;
@@ -351,11 +367,16 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
       // contribution arrives scaled exactly (w 2^s rounds like w)
       const int  jb = -joff[0] - joff[1] * G::WJ0 - joff[2] * (G::WJ0 * G::WJ1);
       const real wp = fixed ? w[p] * scale : w[p];
+      // Shared-memory atomics serialise the lanes of a warp that hit one
+      // word, and cell-sorted lanes share their boxes: odd and even lanes
+      // add to separate copies, which halves those collisions. The flush
+      // sums the copies' integer totals, so J is unchanged to the bit.
+      unsigned* Jc = Jw + (G::COPIES == 2 ? (int)(threadIdx.x & 1) * G::COPY : 0);
       deposit_particle<D, O, real>(q, wp, S.charge, a.inv_dt, a.dx, ng, nullptr,
                                    [&](int i, int j, int k, int c, real v) {
                                      const int e = jb + i + j * G::WJ0 +
                                                    k * (G::WJ0 * G::WJ1) + c * G::NJ;
-                                     if (fixed) FA::add(Jw + e, G::PLANE, v);
+                                     if (fixed) FA::add(Jc + e, G::PLANE, v);
                                      else       atomicAdd(Jr + e, v);
                                    });
     }
@@ -366,8 +387,18 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
   for (int idx = threadIdx.x; idx < 3 * G::NJ; idx += NT) {
     real v;
     if (fixed) {
-      if (!FA::nonzero(Jw + idx, G::PLANE)) continue;
-      v = FA::value(Jw + idx, G::PLANE, unscale);
+      long long t = 0;
+      bool      any = false;
+#pragma unroll
+      for (int k = 0; k < G::COPIES; ++k) {
+        const unsigned* wk = Jw + k * G::COPY + idx;
+        if (FA::nonzero(wk, G::PLANE)) {
+          any = true;
+          t += FA::total(wk, G::PLANE);
+        }
+      }
+      if (!any) continue;
+      v = FA::to_real(t, unscale);
     } else {
       v = Jr[idx];
       if (v == (real)0) continue;
