@@ -89,6 +89,14 @@ class PicInjectParams(C.Structure):
                 ("seed", C.c_uint64), ("first_pair", C.c_uint64)]
 
 
+PIC_FBC_PERIODIC, PIC_FBC_NONE, PIC_FBC_CONDUCTOR, PIC_FBC_MATCH = 0, 1, 2, 3
+
+
+class PicFieldBCs(C.Structure):
+    _fields_ = [("kind", (C.c_int32 * 2) * 3), ("x_min", C.c_double * 3), ("dx", C.c_double),
+                ("match_ds", (C.c_double * 2) * 3), ("match_target", C.c_void_p)]
+
+
 class PicGRParams(C.Structure):
     _fields_ = [("niter", C.c_int32), ("island_lo", C.c_int32), ("island_hi", C.c_int32),
                 ("match_ds", C.c_double), ("match_target", C.c_void_p)]
@@ -137,6 +145,8 @@ SIGNATURES = {
     "pic_particle_moments": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32,
                                        C.POINTER(C.c_double), _VP]),
     "pic_charge_density": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32, _VP, _VP]),
+    "pic_set_field_bcs": (C.c_int, [_VP, C.POINTER(PicFieldBCs)]),
+    "pic_field_boundaries": (C.c_int, [_VP, _VP, C.c_int32, C.c_int32, _VP]),
     "pic_inject_uniform_maxwellians": (C.c_int, [_VP, C.POINTER(PicSpecies),
                                                  C.POINTER(PicSpecies),
                                                  C.POINTER(PicInjectParams),

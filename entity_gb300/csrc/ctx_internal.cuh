@@ -57,6 +57,8 @@ struct pic_ctx {
   std::vector<cudaStream_t>                       gr_side;
   std::vector<cudaEvent_t>                        gr_join;
   cudaEvent_t                                     gr_fork = nullptr;
+  // SR field boundaries (pic_set_field_bcs)
+  pic_field_bcs                                   fbc = {};
 };
 
 namespace pic_internal {

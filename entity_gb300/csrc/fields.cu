@@ -608,6 +608,15 @@ cudaError_t launch_filter(const GridInfo& g, FieldView<real> J, FieldView<real> 
 }
 
 template <typename real>
+cudaError_t launch_copy3(const GridInfo& g, FieldView<real> src, FieldView<real> dst,
+                         cudaStream_t s) {
+  const int64_t ncells_g = (int64_t)(g.n[0] + 2 * g.ng) * (g.n[1] + 2 * g.ng) *
+                           (g.dim == 3 ? g.n[2] + 2 * g.ng : 1) * 3;
+  PIC_KL(k_copy3<real><<<grid_for(ncells_g, 256), 256, 0, s>>>(g, src, dst));
+  return cudaGetLastError();
+}
+
+template <typename real>
 cudaError_t launch_zero3(const GridInfo& g, FieldView<real> f, cudaStream_t s) {
   const int64_t ncells_g = (int64_t)(g.n[0] + 2 * g.ng) * (g.n[1] + 2 * g.ng) *
                            (g.dim == 3 ? g.n[2] + 2 * g.ng : 1) * 3;
@@ -833,6 +842,7 @@ PIC_INST_ADJ_FIELDS(double)
   template cudaError_t launch_filter<R>(const GridInfo&, FieldView<R>, FieldView<R>, int,        \
                                         cudaStream_t);                                           \
   template cudaError_t launch_zero3<R>(const GridInfo&, FieldView<R>, cudaStream_t);             \
+  template cudaError_t launch_copy3<R>(const GridInfo&, FieldView<R>, FieldView<R>, cudaStream_t); \
   template cudaError_t launch_energy<R>(const GridInfo&, FieldView<R>, double, double*,          \
                                         cudaStream_t);
 

@@ -37,6 +37,15 @@ cudaError_t launch_filter(const GridInfo& g, FieldView<real> J, FieldView<real> 
                           cudaStream_t s);
 template <typename real>
 cudaError_t launch_zero3(const GridInfo& g, FieldView<real> f, cudaStream_t s);
+// every cell (ghosts included) of a 3-component field
+template <typename real>
+cudaError_t launch_copy3(const GridInfo& g, FieldView<real> src, FieldView<real> dst,
+                         cudaStream_t s);
+// one filter pass with conductor walls on the flagged sides (field_bcs.cu):
+// reads buff (the pass's copy of J), writes J's active cells
+template <typename real>
+cudaError_t launch_filter_cond(const GridInfo& g, const int lo[3], const int hi[3],
+                               FieldView<real> J, FieldView<real> buff, cudaStream_t s);
 template <typename real>
 cudaError_t launch_energy(const GridInfo& g, FieldView<real> EB, double dx, double* out,
                           cudaStream_t s);

@@ -260,6 +260,38 @@ static std::atomic<long long> g_launches{ 0 };
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 }  // namespace pic
 
+namespace {
+
+// srpic::CurrentsFilter (currents.h:89-119) with conductor walls: each pass
+// copies J to buff, filters with the wall stencils, refills the periodic
+// ghosts (CommunicateFields)
+template <typename real>
+int filter_cond(pic_ctx* c, void* J, void* buff, int npasses, cudaStream_t s) {
+  const auto g = ginfo(c);
+  int        lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = d < g.dim && c->fbc.kind[d][0] == PIC_FBC_CONDUCTOR;
+    hi[d] = d < g.dim && c->fbc.kind[d][1] == PIC_FBC_CONDUCTOR;
+  }
+  const auto Jv = cur_view<real>(c, J), Bv = cur_view<real>(c, buff);
+  for (int p = 0; p < npasses; ++p) {
+    cudaError_t e = pic::launch_copy3<real>(g, Jv, Bv, s);
+    if (e == cudaSuccess) e = pic::launch_filter_cond<real>(g, lo, hi, Jv, Bv, s);
+    if (e == cudaSuccess) e = pic::launch_fill_ghosts<real>(g, Jv, 0, 3, s);
+    if (e != cudaSuccess) return PIC_ERR_CUDA;
+  }
+  return PIC_OK;
+}
+
+bool has_conductor(const pic_ctx* c) {
+  for (int d = 0; d < c->grid.dim; ++d)
+    if (c->fbc.kind[d][0] == PIC_FBC_CONDUCTOR || c->fbc.kind[d][1] == PIC_FBC_CONDUCTOR)
+      return true;
+  return false;
+}
+
+}  // namespace
+
 extern "C" {
 
 int64_t pic_kernel_launches(void) { return (int64_t)pic::g_launches.load(std::memory_order_relaxed); }
@@ -289,6 +321,9 @@ int pic_create(const pic_grid* grid, pic_ctx** out) {
   if (st != PIC_OK) return st;
   pic_ctx* c = new pic_ctx();
   c->grid    = *grid;
+  for (int d = 0; d < 3; ++d)
+    for (int h = 0; h < 2; ++h)
+      c->fbc.kind[d][h] = (d >= grid->dim || grid->fld_periodic[d]) ? PIC_FBC_PERIODIC : PIC_FBC_NONE;
   if (cudaMalloc((void**)&c->d_err, sizeof(unsigned long long) * 4) != cudaSuccess ||
       cudaMalloc((void**)&c->d_energy, sizeof(double) * (2 + PIC_NMOMENTS)) != cudaSuccess) {
     if (c->d_err) cudaFree(c->d_err);
@@ -561,6 +596,9 @@ int pic_filter_currents(pic_ctx* c, void* J, void* buff, int32_t npasses, void* 
   if (!c || !J || npasses < 0) return PIC_ERR_ARG;
   if (npasses == 0) return PIC_OK;
   if (!buff) return PIC_ERR_ARG;
+  if (has_conductor(c))
+    return is_f64(c) ? filter_cond<double>(c, J, buff, npasses, strm(stream))
+                     : filter_cond<float>(c, J, buff, npasses, strm(stream));
   if (is_f64(c))
     return cuda_status(pic::launch_filter<double>(ginfo(c), cur_view<double>(c, J), cur_view<double>(c, buff),
                                                   npasses, strm(stream)));

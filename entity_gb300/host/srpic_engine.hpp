@@ -99,7 +99,7 @@ inline int SortParticles(Domain& dom, const pic_step_params& p, int64_t step, vo
   return PIC_OK;
 }
 
-// SRPICEngine::step_forward (srpic.hpp:65-188), periodic Cartesian domain
+// SRPICEngine::step_forward (srpic.hpp:65-188), Cartesian domain
 template <typename real>
 int StepForward(Domain& dom, const pic_step_params& p, int64_t step, void* stream) {
   int st;
@@ -118,6 +118,8 @@ int StepForward(Domain& dom, const pic_step_params& p, int64_t step, void* strea
   if (fs) {
     PIC_TRY(mark(PIC_PHASE_FIELDSOLVER, 0));
     PIC_TRY(Faraday<real>(dom, p, (real)0.5, stream));
+    // FieldBoundaries(BC::B) (srpic.hpp:94-101); no launch on periodic sides
+    PIC_TRY(pic_field_boundaries(dom.ctx, dom.EB, 0, 1, stream));
     PIC_TRY(mark(PIC_PHASE_FIELDSOLVER, 1));
   }
   PIC_TRY(mark(PIC_PHASE_PUSH_DEPOSIT, 0));
@@ -134,7 +136,10 @@ int StepForward(Domain& dom, const pic_step_params& p, int64_t step, void* strea
   if (fs) {
     PIC_TRY(mark(PIC_PHASE_FIELDSOLVER, 0));
     PIC_TRY(Faraday<real>(dom, p, (real)0.5, stream));
+    PIC_TRY(pic_field_boundaries(dom.ctx, dom.EB, 0, 1, stream));
     PIC_TRY(AmpereWithCurrents<real>(dom, p, (real)1, dep, stream));
+    // FieldBoundaries(BC::E) (srpic.hpp:169-176)
+    PIC_TRY(pic_field_boundaries(dom.ctx, dom.EB, 1, 0, stream));
     PIC_TRY(mark(PIC_PHASE_FIELDSOLVER, 1));
   }
   PIC_TRY(mark(PIC_PHASE_SORT, 0));

@@ -177,6 +177,26 @@ class Context:
         arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
         abi.call("pic_charge_density", self.h, arr, len(species), _ptr(rho), _stream_ptr(stream))
 
+    def set_field_bcs(self, kinds, x_min=(0.0, 0.0, 0.0), dx=1.0, match_ds=None, target=None):
+        """pic_set_field_bcs: kinds = ((min, max), ...) per axis of
+        abi.PIC_FBC_*; MATCH sides need match_ds ((min, max), ...) and the
+        target field (kept alive by the caller)."""
+        b = abi.PicFieldBCs()
+        for d in range(3):
+            for h in range(2):
+                b.kind[d][h] = kinds[d][h] if d < len(kinds) else abi.PIC_FBC_PERIODIC
+                if match_ds is not None and d < len(match_ds):
+                    b.match_ds[d][h] = match_ds[d][h]
+            b.x_min[d] = x_min[d] if d < len(x_min) else 0.0
+        b.dx = dx
+        b.match_target = target.data_ptr() if target is not None else None
+        self._fbc_target = target
+        abi.call("pic_set_field_bcs", self.h, C.byref(b))
+
+    def field_boundaries(self, EB, set_e, set_b, stream=None):
+        abi.call("pic_field_boundaries", self.h, _ptr(EB), int(set_e), int(set_b),
+                 _stream_ptr(stream))
+
     def inject_uniform_maxwellians(self, sp1: SpeciesArrays, sp2: SpeciesArrays, params,
                                    stream=None):
         """pic_inject_uniform_maxwellians: appends the pairs to both species

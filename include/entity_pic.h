@@ -501,6 +501,44 @@ int pic_grpic_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, int32_
                    void* fields[6], const pic_step_params* prm, const pic_gr_params* gprm,
                    int64_t step, void* stream);
 
+/* ---- SR field boundaries ---------------------------------------------- */
+
+/* grid.boundaries.fields, per side; PERIODIC exactly on the axes the grid
+ * was created periodic on. NONE leaves the ghost cells as they are (the
+ * default of a non-periodic axis). */
+#define PIC_FBC_PERIODIC 0
+#define PIC_FBC_NONE 1
+#define PIC_FBC_CONDUCTOR 2
+#define PIC_FBC_MATCH 3
+
+typedef struct {
+  int32_t     kind[3][2];     /* PIC_FBC_* for (min, max) of each axis */
+  double      x_min[3];       /* physical lower edge per axis (MATCH's coordinate) */
+  double      dx;             /* cell size (MATCH) */
+  double      match_ds[3][2]; /* grid.boundaries.match.ds per side (MATCH) */
+  const void* match_target;   /* field MATCH relaxes toward, em layout (the
+                                 problem generator's MatchFields, kept current
+                                 by the caller) */
+} pic_field_bcs;
+
+/* Sets the context's field boundaries. PERIODIC must sit on the grid's
+ * periodic axes. A context starts with PERIODIC there and NONE elsewhere. */
+int pic_set_field_bcs(pic_ctx* ctx, const pic_field_bcs* bcs);
+
+/* srpic::FieldBoundaries (src/engines/srpic/fields_bcs.h:622-672) on EB for
+ * the E (set_e) and/or B (set_b) components, sides in Directions<D>::orth
+ * order:
+ *  - CONDUCTOR: ConductorBoundaries_kernel (src/kernels/fields_bcs.hpp:
+ *    522-800): tangential E and normal B vanish on the wall, ghosts mirror
+ *    the active cells;
+ *  - MATCH: MatchBoundaries_kernel, SRPIC branch (fields_bcs.hpp:42-520):
+ *    F = s F + (1 - s) target over the match layer, s = tanh(4 |x - x_edge|
+ *    / ds) at each component's position.
+ * pic_srpic_step calls it after each Faraday half (B) and after Ampere (E).
+ * With conductor walls the current filter also takes the reference's wall
+ * stencils (digital_filter.hpp:129-379). */
+int pic_field_boundaries(pic_ctx* ctx, void* EB, int32_t set_e, int32_t set_b, void* stream);
+
 /* ---- particle injection ------------------------------------------------ */
 
 /* Parameters of arch::InjectUniformMaxwellians (src/archetypes/utils.h:46-107)

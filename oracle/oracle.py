@@ -18,6 +18,7 @@ class OrcGrid(C.Structure):
         ("dim", C.c_int), ("n1", C.c_int), ("n2", C.c_int), ("n3", C.c_int), ("ng", C.c_int),
         ("em_s", C.c_int64 * 4), ("cur_s", C.c_int64 * 4),
         ("periodic", C.c_int * 3), ("prtl_bc", (C.c_int * 2) * 3),
+        ("fbc", (C.c_int * 2) * 3),
     ]
 
 
@@ -96,6 +97,8 @@ def lib(real):
         L.orc_kinetic_energy.argtypes = [S]
         L.orc_charge_density.argtypes = [G, S, V, C.c_int]
         L.orc_particle_moments.argtypes = [S, C.POINTER(C.c_double)]
+        L.orc_field_boundaries.argtypes = [G, V, C.c_int, C.c_int, V, C.c_double * 3,
+                                           C.c_double, (C.c_double * 2) * 3]
         L.orc_max_threads.restype = C.c_int
         L.orc_real_size.restype = C.c_int
         P = C.POINTER(OrcInjectParams)
@@ -131,7 +134,10 @@ class Oracle:
             og.periodic[d] = int(g.periodic[d]) if d < g.dim else 0
             og.prtl_bc[d][0] = g.prtl_bc[d][0]
             og.prtl_bc[d][1] = g.prtl_bc[d][1]
+            for h in range(2):
+                og.fbc[d][h] = 0 if (d >= g.dim or g.periodic[d]) else 1
         self.og = og
+        self.fbc_args = None
 
     def species(self, sp):
         os_ = OrcSpecies()
@@ -144,6 +150,26 @@ class Oracle:
         os_.weight, os_.tag = _p(sp.w), _p(sp.tag)
         os_.npart, os_.mass, os_.charge, os_.pusher = sp.npart, sp.mass, sp.charge, sp.pusher
         return os_
+
+    def set_field_bcs(self, kinds, x_min=(0.0, 0.0, 0.0), dx=1.0, match_ds=None, target=None):
+        """Field boundary kinds per side (0 periodic, 1 none, 2 conductor,
+        3 match), as the product's pic_set_field_bcs."""
+        for d in range(len(kinds)):
+            for h in range(2):
+                self.og.fbc[d][h] = kinds[d][h]
+        ds = ((C.c_double * 2) * 3)()
+        for d in range(3):
+            for h in range(2):
+                ds[d][h] = match_ds[d][h] if (match_ds is not None and d < len(match_ds)) else 0.0
+        xm = (C.c_double * 3)(*[x_min[d] if d < len(x_min) else 0.0 for d in range(3)])
+        self.fbc_args = (target, xm, dx, ds)
+
+    def field_boundaries(self, EB, set_e, set_b):
+        if not any(self.og.fbc[d][h] >= 2 for d in range(3) for h in range(2)):
+            return
+        target, xm, dx, ds = self.fbc_args
+        self.L.orc_field_boundaries(C.byref(self.og), _p(EB), int(set_e), int(set_b), _p(target),
+                                    xm, dx, ds)
 
     def inject_uniform(self, sp1, sp2, params):
         """Appends the injected pairs (both species' npart advance); returns
@@ -242,6 +268,7 @@ class Oracle:
         if prm.fieldsolver_enabled:
             self.faraday(EB, float(c1), float(c2))
             self.fill_ghosts(EB, True, 3, 6)
+            self.field_boundaries(EB, 0, 1)
         for sp in species:
             if sp.pusher != 0 and sp.npart > 0:
                 self.push(sp, EB, prm.dt, prm.omegaB0, prm.dx)
@@ -255,6 +282,7 @@ class Oracle:
         if prm.fieldsolver_enabled:
             self.faraday(EB, float(c1), float(c2))
             self.fill_ghosts(EB, True, 3, 6)
+            self.field_boundaries(EB, 0, 1)
             dT1 = t(1.0) * t(prm.correction) * t(prm.dt)
             a1 = dT1 / (dxm * dxm) if g.dim == 2 else dT1 / dxm
             a2 = dT1 if g.dim == 2 else t(0.0)
@@ -266,6 +294,7 @@ class Oracle:
                 self.fill_ghosts(J, False, 0, 3)
             else:
                 self.fill_ghosts(EB, True, 0, 3)
+            self.field_boundaries(EB, 1, 0)
         for sp in species:
             if prm.clear_interval > 0 and step % prm.clear_interval == 0 and step > 0:
                 self.remove_dead(sp)

@@ -55,6 +55,17 @@ int orc_real_size(void) { return (int)sizeof(real); }
   ((int64_t)(i) * (g)->cur_s[0] + (int64_t)(j) * (g)->cur_s[1] +               \
    (int64_t)(k) * (g)->cur_s[2] + (int64_t)(c) * (g)->cur_s[3])
 
+/* EB index of the cell at `i` along `axis` and (pa, pb) along the two other
+ * axes (oa < ob) */
+static int64_t cond_idx(const orc_grid* g, int axis, int oa, int ob, int i, int pa, int pb,
+                        int c) {
+  int x[3] = { 0, 0, 0 };
+  x[axis] = i;
+  x[oa]   = pa;
+  if (g->dim == 3) x[ob] = pb;
+  return EBI(g, x[0], x[1], x[2], c);
+}
+
 static int ext(const orc_grid* g, int d) {
   const int n = d == 0 ? g->n1 : (d == 1 ? g->n2 : g->n3);
   return (d < g->dim) ? n + 2 * g->ng : 1;
@@ -883,6 +894,100 @@ void orc_currents_ampere(const orc_grid* g, void* EBv, void* Jv, double coeff_d,
 /* ------------------------------------------------------------------------ */
 /* digital filter: src/kernels/digital_filter.hpp:183-195, 352-379           */
 /* ------------------------------------------------------------------------ */
+/* DigitalFilter_kernel with conductor walls (digital_filter.hpp:99-379) for
+ * one active cell: the first matching wall case in the order x1, x2, x3
+ * writes the components the reference writes; other cells take the full
+ * stencil. The wall's inner neighbour index is i + 1 whenever the lower side
+ * is a conductor, as the reference picks it. Returns 0 when no wall case
+ * applies. */
+static int filter_cond_cell(const orc_grid* g, real* J, const real* B, int i1, int i2, int i3) {
+  const int c1l = g->fbc[0][0] == 2, c1h = g->fbc[0][1] == 2;
+  const int c2l = g->fbc[1][0] == 2, c2h = g->fbc[1][1] == 2;
+  const int c3l = g->dim == 3 && g->fbc[2][0] == 2, c3h = g->dim == 3 && g->fbc[2][1] == 2;
+  const int i1min = g->ng, i1max = g->n1 + g->ng, i2min = g->ng, i2max = g->n2 + g->ng;
+  const int i3min = g->ng, i3max = g->n3 + g->ng;
+  const real THREE = 3;
+#define bb(x, y, z, c) B[JI(g, x, y, z, c)]
+#define aa(c)          J[JI(g, i1, i2, i3, c)]
+  if (g->dim == 2) {
+#define FI1(c, I, Jj) (INV_2 * bb((I), (Jj), 0, c) + INV_4 * (bb((I) - 1, (Jj), 0, c) + bb((I) + 1, (Jj), 0, c)))
+#define FI2(c, I, Jj) (INV_2 * bb((I), (Jj), 0, c) + INV_4 * (bb((I), (Jj) - 1, 0, c) + bb((I), (Jj) + 1, 0, c)))
+    if ((c1l && i1 == i1min) || (c1h && i1 == i1max - 1)) {
+      const int s = c1l ? i1 + 1 : i1 - 1;
+      aa(0) = (THREE * INV_4) * (FI2(0, i1, i2)) + (INV_4) * (FI2(0, s, i2));
+    } else if ((c1l && i1 == i1min + 1) || (c1h && i1 == i1max - 2)) {
+      const int s = c1l ? i1 + 1 : i1 - 1;
+      aa(0) = INV_2 * (FI2(0, i1, i2)) + INV_4 * ((FI2(0, i1 - 1, i2)) + (FI2(0, i1 + 1, i2)));
+      aa(1) = (INV_2) * (FI2(1, i1, i2)) + (INV_4) * (FI2(1, s, i2));
+      aa(2) = (INV_2) * (FI2(2, i1, i2)) + (INV_4) * (FI2(2, s, i2));
+    } else if ((c2l && i2 == i2min) || (c2h && i2 == i2max - 1)) {
+      const int s = c2l ? i2 + 1 : i2 - 1;
+      aa(1) = (THREE * INV_4) * (FI1(1, i1, i2)) + (INV_4) * (FI1(1, i1, s));
+    } else if ((c2l && i2 == i2min + 1) || (c2h && i2 == i2max - 2)) {
+      const int s = c2l ? i2 + 1 : i2 - 1;
+      aa(0) = INV_2 * (FI1(0, i1, i2)) + INV_4 * (FI1(0, i1, s));
+      aa(1) = INV_2 * (FI1(1, i1, i2)) + INV_4 * ((FI1(1, i1, i2 - 1)) + (FI1(1, i1, i2 + 1)));
+      aa(2) = INV_2 * (FI1(2, i1, i2)) + INV_4 * (FI1(2, i1, s));
+    } else {
+      return 0;
+    }
+#undef FI1
+#undef FI2
+    return 1;
+  }
+#define P23(c, I, Jj, K)                                                                       \
+  (INV_4 * bb(I, Jj, K, c) +                                                                   \
+   INV_8 * (bb((I), (Jj) - 1, (K), c) + bb((I), (Jj) + 1, (K), c) + bb((I), (Jj), (K) - 1, c) + \
+            bb((I), (Jj), (K) + 1, c)) +                                                       \
+   INV_16 * (bb((I), (Jj) - 1, (K) - 1, c) + bb((I), (Jj) + 1, (K) + 1, c) +                   \
+             bb((I), (Jj) - 1, (K) + 1, c) + bb((I), (Jj) + 1, (K) - 1, c)))
+#define P13(c, I, Jj, K)                                                                       \
+  (INV_4 * bb(I, Jj, K, c) +                                                                   \
+   INV_8 * (bb((I) - 1, (Jj), (K), c) + bb((I) + 1, (Jj), (K), c) + bb((I), (Jj), (K) - 1, c) + \
+            bb((I), (Jj), (K) + 1, c)) +                                                       \
+   INV_16 * (bb((I) - 1, (Jj), (K) - 1, c) + bb((I) + 1, (Jj), (K) + 1, c) +                   \
+             bb((I) - 1, (Jj), (K) + 1, c) + bb((I) + 1, (Jj), (K) - 1, c)))
+#define P12(c, I, Jj, K)                                                                       \
+  (INV_4 * bb(I, Jj, K, c) +                                                                   \
+   INV_8 * (bb((I) - 1, (Jj), (K), c) + bb((I) + 1, (Jj), (K), c) + bb((I), (Jj) - 1, (K), c) + \
+            bb((I), (Jj) + 1, (K), c)) +                                                       \
+   INV_16 * (bb((I) - 1, (Jj) - 1, (K), c) + bb((I) + 1, (Jj) + 1, (K), c) +                   \
+             bb((I) - 1, (Jj) + 1, (K), c) + bb((I) + 1, (Jj) - 1, (K), c)))
+  if ((c1l && i1 == i1min) || (c1h && i1 == i1max - 1)) {
+    const int s = c1l ? i1 + 1 : i1 - 1;
+    aa(0) = (THREE * INV_4) * (P23(0, i1, i2, i3)) + (INV_4) * (P23(0, s, i2, i3));
+  } else if ((c1l && i1 == i1min + 1) || (c1h && i1 == i1max - 2)) {
+    const int s = c1l ? i1 + 1 : i1 - 1;
+    aa(0) = INV_2 * (P23(0, i1, i2, i3)) + INV_4 * ((P23(0, i1 - 1, i2, i3)) + (P23(0, i1 + 1, i2, i3)));
+    aa(1) = INV_2 * (P23(1, i1, i2, i3)) + INV_4 * (P23(1, s, i2, i3));
+    aa(2) = INV_2 * (P23(2, i1, i2, i3)) + INV_4 * (P23(2, s, i2, i3));
+  } else if ((c2l && i2 == i2min) || (c2h && i2 == i2max - 1)) {
+    const int s = c2l ? i2 + 1 : i2 - 1;
+    aa(1) = (THREE * INV_4) * (P13(1, i1, i2, i3)) + (INV_4) * (P13(1, i1, s, i3));
+  } else if ((c2l && i2 == i2min + 1) || (c2h && i2 == i2max - 2)) {
+    const int s = c2l ? i2 + 1 : i2 - 1;
+    aa(0) = INV_2 * (P13(0, i1, i2, i3)) + INV_4 * (P13(0, i1, s, i3));
+    aa(1) = INV_2 * (P13(1, i1, i2, i3)) + INV_4 * ((P13(1, i1, i2 - 1, i3)) + (P13(1, i1, i2 + 1, i3)));
+    aa(2) = INV_2 * (P13(2, i1, i2, i3)) + INV_4 * (P13(2, i1, s, i3));
+  } else if ((c3l && i3 == i3min) || (c3h && i3 == i3max - 1)) {
+    const int s = c3l ? i3 + 1 : i3 - 1;
+    aa(2) = (THREE * INV_4) * (P12(2, i1, i2, i3)) + (INV_4) * (P12(2, i1, i2, s));
+  } else if ((c3l && i3 == i3min + 1) || (c3h && i3 == i3max - 2)) {
+    const int s = c3l ? i3 + 1 : i3 - 1;
+    aa(0) = INV_2 * (P12(0, i1, i2, i3)) + INV_4 * (P12(0, i1, i2, s));
+    aa(1) = INV_2 * (P12(1, i1, i2, i3)) + INV_4 * (P12(1, i1, i2, s));
+    aa(2) = INV_2 * (P12(2, i1, i2, i3)) + INV_4 * ((P12(2, i1, i2, i3 - 1)) + (P12(2, i1, i2, i3 + 1)));
+  } else {
+    return 0;
+  }
+#undef P23
+#undef P13
+#undef P12
+#undef aa
+#undef bb
+  return 1;
+}
+
 void orc_filter_pass(const orc_grid* g, void* Jv, void* buffv) {
   real*         J  = (real*)Jv;
   real*         B  = (real*)buffv;
@@ -898,6 +1003,7 @@ void orc_filter_pass(const orc_grid* g, void* Jv, void* buffv) {
 #pragma omp parallel for schedule(static)
     for (int i2 = ng; i2 < g->n2 + ng; ++i2) {
       for (int i1 = ng; i1 < g->n1 + ng; ++i1) {
+        if (filter_cond_cell(g, J, B, i1, i2, 0)) continue;
         for (int c = 0; c < 3; ++c) {
 #define b(a, bb) B[JI(g, a, bb, 0, c)]
           J[JI(g, i1, i2, 0, c)] =
@@ -914,6 +1020,7 @@ void orc_filter_pass(const orc_grid* g, void* Jv, void* buffv) {
     for (int i3 = ng; i3 < g->n3 + ng; ++i3) {
       for (int i2 = ng; i2 < g->n2 + ng; ++i2) {
         for (int i1 = ng; i1 < g->n1 + ng; ++i1) {
+          if (filter_cond_cell(g, J, B, i1, i2, i3)) continue;
           for (int c = 0; c < 3; ++c) {
 #define b(x, y, z) B[JI(g, x, y, z, c)]
             /* the (i, j, k +- 1) pair appears twice in the 1/32 group, as in
@@ -1235,5 +1342,116 @@ void orc_particle_moments(const orc_species* sp, double* out) {
     out[3] += c;
     out[4] += (double)w[p] * (m == 0.0 ? sqrt(u2s) : m * (u2s / (gm + 1.0)));
     out[5] += (double)w[p];
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* SR field boundaries                                                      */
+/* ------------------------------------------------------------------------ */
+/* ConductorBoundaries_kernel (fields_bcs.hpp:522-800) on one side: offsets
+ * k from the wall cell, over [0, ng + 1) below and [0, ng) above */
+static void conductor_side(const orc_grid* g, real* F, int axis, int hi, int set_e, int set_b) {
+  const int ng = g->ng, n = axis == 0 ? g->n1 : (axis == 1 ? g->n2 : g->n3);
+  const int edge = hi ? n + ng : ng, K = hi ? ng : ng + 1;
+  const int oa = axis == 0 ? 1 : 0, ob = axis == 2 ? 1 : 2;
+  const int t1 = oa, t2 = g->dim == 3 ? ob : 2;
+  const int ea = ext(g, oa), eb = g->dim == 3 ? ext(g, ob) : 1;
+  for (int pb = 0; pb < eb; ++pb)
+    for (int pa = 0; pa < ea; ++pa)
+      for (int k = 0; k < K; ++k) {
+#define AT(i, c) F[cond_idx(g, axis, oa, ob, i, pa, pb, c)]
+        if (set_e) {
+          if (k == 0) {
+            AT(edge, t1) = 0;
+            AT(edge, t2) = 0;
+          } else if (!hi) {
+            AT(edge - k, axis) = AT(edge + k - 1, axis);
+            AT(edge - k, t1)   = -AT(edge + k, t1);
+            AT(edge - k, t2)   = -AT(edge + k, t2);
+          } else {
+            AT(edge + k - 1, axis) = AT(edge - k, axis);
+            AT(edge + k, t1)       = -AT(edge - k, t1);
+            AT(edge + k, t2)       = -AT(edge - k, t2);
+          }
+        }
+        if (set_b) {
+          if (k == 0) {
+            AT(edge, 3 + axis) = 0;
+          } else if (!hi) {
+            AT(edge - k, 3 + axis) = -AT(edge + k, 3 + axis);
+            AT(edge - k, 3 + t1)   = AT(edge + k - 1, 3 + t1);
+            AT(edge - k, 3 + t2)   = AT(edge + k - 1, 3 + t2);
+          } else {
+            AT(edge + k, 3 + axis)   = -AT(edge - k, 3 + axis);
+            AT(edge + k - 1, 3 + t1) = AT(edge - k, 3 + t1);
+            AT(edge + k - 1, 3 + t2) = AT(edge - k, 3 + t2);
+          }
+        }
+#undef AT
+      }
+}
+
+/* MatchBoundaries_kernel, SRPIC branch, on one side over the cells that
+ * MatchFieldsIn / ExtentToRange select (srpic/fields_bcs.h:60-202, mesh.h:
+ * 133-202) */
+static void match_side(const orc_grid* g, real* F, const real* T, int axis, int hi, int set_e,
+                       int set_b, const double x_min[3], double dx_d, double ds_d) {
+  const int  ng = g->ng, n = axis == 0 ? g->n1 : (axis == 1 ? g->n2 : g->n3);
+  const real dx = (real)dx_d, x0 = (real)x_min[axis], x1 = x0 + (real)n * dx, ds = (real)ds_d;
+  real       lo_x = hi ? x1 - ds : x0, hi_x = hi ? x1 : x0 + ds;
+  lo_x = lo_x < x0 ? x0 : (lo_x > x1 ? x1 : lo_x);
+  hi_x = hi_x > x1 ? x1 : (hi_x < x0 ? x0 : hi_x);
+#ifdef ORC_SINGLE
+  real a = floorf((lo_x - x0) / dx), e = ceilf((hi_x - x0) / dx);
+#else
+  real a = floor((lo_x - x0) / dx), e = ceil((hi_x - x0) / dx);
+#endif
+  int i0, i1;
+  if (hi) {
+    if (a < 0) a = 0;
+    i0 = (int)a + ng;
+    i1 = (int)e + 2 * ng;
+  } else {
+    if (e > (real)n) e = (real)n;
+    i0 = (int)a;
+    i1 = (int)e + ng;
+  }
+  if (i0 < 0) i0 = 0;
+  if (i1 > n + 2 * ng) i1 = n + 2 * ng;
+  const real x_edge = hi ? x1 : x0, ONE = 1, FOUR = 4, H = 0.5;
+  const int  oa = axis == 0 ? 1 : 0, ob = axis == 2 ? 1 : 2;
+  const int  ea = ext(g, oa), eb = g->dim == 3 ? ext(g, ob) : 1;
+  for (int i = i0; i < i1; ++i) {
+    const real i_ = (real)(i - ng);
+#ifdef ORC_SINGLE
+    const real s0 = tanhf(fabsf((x0 + i_ * dx) - x_edge) * FOUR / ds);
+    const real sH = tanhf(fabsf((x0 + (i_ + H) * dx) - x_edge) * FOUR / ds);
+#else
+    const real s0 = tanh(fabs((x0 + i_ * dx) - x_edge) * FOUR / ds);
+    const real sH = tanh(fabs((x0 + (i_ + H) * dx) - x_edge) * FOUR / ds);
+#endif
+    for (int pb = 0; pb < eb; ++pb)
+      for (int pa = 0; pa < ea; ++pa)
+        for (int c = 0; c < 6; ++c) {
+          if (c < 3 ? !set_e : !set_b) continue;
+          const int  half = c < 3 ? (c == axis) : (c - 3 != axis);
+          const real s    = half ? sH : s0;
+          const int64_t q = cond_idx(g, axis, oa, ob, i, pa, pb, c);
+          F[q] = s * F[q] + (ONE - s) * T[q];
+        }
+  }
+}
+
+void orc_field_boundaries(const orc_grid* g, void* EB, int set_e, int set_b, const void* target,
+                          const double x_min[3], double dx, const double ds[3][2]) {
+  real* F = (real*)EB;
+  int   order[6][2], m = 0;
+  for (int d = 0; d < g->dim; ++d) order[m][0] = d, order[m++][1] = 0;
+  for (int d = g->dim - 1; d >= 0; --d) order[m][0] = d, order[m++][1] = 1;
+  for (int k = 0; k < m; ++k) {
+    const int axis = order[k][0], hi = order[k][1], kind = g->fbc[axis][hi];
+    if (kind == 2) conductor_side(g, F, axis, hi, set_e, set_b);
+    else if (kind == 3)
+      match_side(g, F, (const real*)target, axis, hi, set_e, set_b, x_min, dx, ds[axis][hi]);
   }
 }

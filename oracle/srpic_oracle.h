@@ -41,6 +41,8 @@ typedef struct {
   int     periodic[3];
   /* particle boundary per side: 0 periodic, 1 absorb, 2 reflect, 3 axis */
   int     prtl_bc[3][2];
+  /* field boundary per side: 0 periodic, 1 none, 2 conductor, 3 match */
+  int     fbc[3][2];
 } orc_grid;
 
 /* one species, structure of arrays (src/framework/containers/particles.h:47-71) */
@@ -75,6 +77,14 @@ int64_t orc_push(const orc_grid* g, orc_species* sp, const void* EB, int order,
  * accumulating into J (does not zero it). */
 void orc_deposit(const orc_grid* g, const orc_species* sp, void* J, int order,
                  double dt, double dx);
+
+/* srpic::FieldBoundaries (src/engines/srpic/fields_bcs.h:622-672) for the
+ * conductor and match sides of g->fbc, in Directions<D>::orth order:
+ * ConductorBoundaries_kernel (src/kernels/fields_bcs.hpp:522-800) and the
+ * SRPIC branch of MatchBoundaries_kernel (fields_bcs.hpp:42-520) relaxing
+ * toward `target` with s = tanh(4 |x - x_edge| / ds), x = x_min + x_Cd dx. */
+void orc_field_boundaries(const orc_grid* g, void* EB, int set_e, int set_b, const void* target,
+                          const double x_min[3], double dx, const double ds[3][2]);
 
 /* kernel::mink::Faraday_kernel (src/kernels/faraday_mink.hpp:71-166) over the
  * active cells. stencil = {deltax, deltay, betaxy, betayx, deltaz, betaxz,
