@@ -91,6 +91,16 @@ class PicInjectParams(C.Structure):
 
 PIC_FBC_PERIODIC, PIC_FBC_NONE, PIC_FBC_CONDUCTOR, PIC_FBC_MATCH = 0, 1, 2, 3
 
+PIC_MOM_RHO, PIC_MOM_CHARGE, PIC_MOM_N, PIC_MOM_NPPC, PIC_MOM_T, PIC_MOM_V = range(6)
+PIC_SMOOTH_CONST, PIC_SMOOTH_SPLINE = 1, 2
+PIC_OUT_INTERP_EDGES, PIC_OUT_INTERP_FACES, PIC_OUT_TO_HAT = 1, 2, 4
+
+
+class PicMomentParams(C.Structure):
+    _fields_ = [("id", C.c_int32), ("c1", C.c_int32), ("c2", C.c_int32), ("order", C.c_int32),
+                ("smoothing", C.c_int32), ("use_weights", C.c_int32), ("inv_n0", C.c_double),
+                ("dx", C.c_double)]
+
 
 class PicFieldBCs(C.Structure):
     _fields_ = [("kind", (C.c_int32 * 2) * 3), ("x_min", C.c_double * 3), ("dx", C.c_double),
@@ -147,6 +157,17 @@ SIGNATURES = {
     "pic_charge_density": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32, _VP, _VP]),
     "pic_set_field_bcs": (C.c_int, [_VP, C.POINTER(PicFieldBCs)]),
     "pic_field_boundaries": (C.c_int, [_VP, _VP, C.c_int32, C.c_int32, _VP]),
+    "pic_output_moment": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32,
+                                    C.POINTER(PicMomentParams), _VP, C.c_int32, _VP]),
+    "pic_sync_moments": (C.c_int, [_VP, _VP, C.c_int32, C.c_int32, _VP]),
+    "pic_normalize_by_rho": (C.c_int, [_VP, _VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                       _VP]),
+    "pic_output_divergence": (C.c_int, [_VP, _VP, _VP, C.c_int32, _VP]),
+    "pic_output_field": (C.c_int, [_VP, _VP, C.c_int32, C.c_int32, C.c_int32, C.c_uint32,
+                                   C.c_double, C.POINTER(C.c_int32), _VP, _VP]),
+    "pic_output_particles": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int64, C.c_double,
+                                       C.POINTER(C.c_double), C.POINTER(_VP), C.POINTER(_VP),
+                                       _VP, C.POINTER(C.c_int64), _VP]),
     "pic_inject_uniform_maxwellians": (C.c_int, [_VP, C.POINTER(PicSpecies),
                                                  C.POINTER(PicSpecies),
                                                  C.POINTER(PicInjectParams),

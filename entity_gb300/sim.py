@@ -208,6 +208,43 @@ class Context:
         sp1.npart, sp2.npart = p1.npart, p2.npart
         return n.value
 
+    def output_moment(self, species, params, bckp, comp, stream=None):
+        """pic_output_moment: adds the moment of `params` (abi.PicMomentParams)
+        of the species into bckp[comp] (EB layout)."""
+        arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])
+        abi.call("pic_output_moment", self.h, arr, len(species), C.byref(params), _ptr(bckp),
+                 int(comp), _stream_ptr(stream))
+
+    def sync_moments(self, bckp, c0, c1, stream=None):
+        abi.call("pic_sync_moments", self.h, _ptr(bckp), int(c0), int(c1), _stream_ptr(stream))
+
+    def normalize_by_rho(self, bckp, c_rho, cv, stream=None):
+        abi.call("pic_normalize_by_rho", self.h, _ptr(bckp), int(c_rho), int(cv[0]), int(cv[1]),
+                 int(cv[2]), _stream_ptr(stream))
+
+    def output_divergence(self, EB, bckp, comp, stream=None):
+        abi.call("pic_output_divergence", self.h, _ptr(EB), _ptr(bckp), int(comp),
+                 _stream_ptr(stream))
+
+    def output_field(self, src, is_em, c0, ncomp, flags, dx, dwn, out, stream=None):
+        """pic_output_field into `out`, a device tensor of
+        ncomp x ceil(n3/d3) x ceil(n2/d2) x ceil(n1/d1) (2D: no n3 axis)."""
+        d = (C.c_int32 * 3)(*[int(x) for x in (list(dwn) + [1, 1, 1])[:3]])
+        abi.call("pic_output_field", self.h, _ptr(src), int(is_em), int(c0), int(ncomp),
+                 int(flags), float(dx), d, _ptr(out), _stream_ptr(stream))
+
+    def output_particles(self, sp: SpeciesArrays, stride, dx, xmin, x, u, w, stream=None):
+        """pic_output_particles: writes npart // stride records into the
+        device tensors x (dim of them), u (3) and w; returns the count."""
+        ps = make_species(sp, self.g.dim)
+        xm = (C.c_double * 3)(*[float(v) for v in (list(xmin) + [0.0, 0.0, 0.0])[:3]])
+        xp = (C.c_void_p * 3)(*[(_ptr(x[d]) if d < len(x) else None) for d in range(3)])
+        up = (C.c_void_p * 3)(*[_ptr(t) for t in u])
+        n = C.c_int64(0)
+        abi.call("pic_output_particles", self.h, C.byref(ps), int(stride), float(dx), xm, xp, up,
+                 _ptr(w), C.byref(n), _stream_ptr(stream))
+        return n.value
+
     def device_errors(self, reset=False, stream=None):
         out = (C.c_int64 * 4)()
         abi.call("pic_get_device_errors", self.h, out, int(reset), _stream_ptr(stream))

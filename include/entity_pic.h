@@ -582,6 +582,96 @@ int pic_gr_inject_uniform_maxwellians(pic_ctx* ctx, const pic_gr_metric* m, pic_
                                       pic_species* sp2, const pic_inject_params* prm, double V0,
                                       int64_t* n_pairs, void* stream);
 
+/* ---- output preparation (SR, Cartesian) -------------------------------- */
+
+/* moments (FldsID, src/global/enums.h) */
+#define PIC_MOM_RHO 0    /* mass density: contribution m */
+#define PIC_MOM_CHARGE 1 /* charge density: contribution q */
+#define PIC_MOM_N 2      /* number density: contribution 1 */
+#define PIC_MOM_NPPC 3   /* particles per cell: no volume or weight factor */
+#define PIC_MOM_T 4      /* stress-energy component T^{c1 c2} (0 = time) */
+#define PIC_MOM_V 5      /* m u_c1 / u^0, to be divided by Rho (pic_normalize_by_rho) */
+
+/* OutputSmoothingType (src/global/enums.h:405-435) */
+#define PIC_SMOOTH_CONST 1u
+#define PIC_SMOOTH_SPLINE 2u
+
+typedef struct {
+  int32_t id;          /* PIC_MOM_* */
+  int32_t c1, c2;      /* components: T uses both (0..3), V uses c1 (1..3) */
+  int32_t order;       /* output.fields.smoothing.order: window = ceil(order / 2) cells */
+  int32_t smoothing;   /* PIC_SMOOTH_* (output.fields.smoothing.method) */
+  int32_t use_weights; /* particles.use_weights */
+  double  inv_n0;      /* 1 / scales.n0 */
+  double  dx;          /* cell size; Minkowski sqrt(det h) = dx^D */
+} pic_moment_params;
+
+/* ComputeMoments (src/framework/domain/metadomain_io.cpp:123-170) with
+ * ParticleMoments_kernel<SRPIC, Minkowski, F> (src/kernels/particle_moments.hpp:
+ * 44-405): every alive particle of the nspecies species adds
+ *   coeff * prod_d S(|dx_d - (di_d + 1/2)|),  |di_d| <= window,
+ * to component `comp` of `bckp` at the cell i + di (ghosts included), where S
+ * is the spline of the given order (prtl_shape::S1..S6) or the constant
+ * 1 / (2 window + 1), and coeff is the moment's contribution times
+ * inv_n0 / dx^D (and the weight with use_weights; neither for Nppc). bckp
+ * has the EB layout (em_stride, 6 components); the caller zeroes it and folds
+ * the ghosts with pic_sync_moments. Sums run in no fixed order (atomics), like
+ * the reference's ScatterView. Particles whose cell lies outside the grid are
+ * skipped and counted in the error word's out[1]. PIC_ERR_ARG: Rho or Charge
+ * of a massless species, window > ng, an unknown smoothing; orders above 6
+ * return PIC_ERR_UNSUPPORTED. */
+int pic_output_moment(pic_ctx* ctx, const pic_species* sp, int32_t nspecies,
+                      const pic_moment_params* prm, void* bckp, int32_t comp, void* stream);
+
+/* Metadomain::SynchronizeFields(domain, Comm::Bckp, {c0, c1})
+ * (src/framework/domain/metadomain_comm.cpp:408-562) along periodic axes:
+ * the active cells add their ghost images of components [c0, c1). The
+ * ghosts are zero afterwards (the reference leaves them as they were; output
+ * reads active cells only). */
+int pic_sync_moments(pic_ctx* ctx, void* bckp, int32_t c0, int32_t c1, void* stream);
+
+/* NormalizeVectorByRho_kernel (src/kernels/particle_moments.hpp:407-478) on
+ * the active cells: components c_v1..c_v3 are divided by c_rho where
+ * |rho| > the real type's epsilon. */
+int pic_normalize_by_rho(pic_ctx* ctx, void* bckp, int32_t c_rho, int32_t c_v1, int32_t c_v2,
+                         int32_t c_v3, void* stream);
+
+/* The divE output: ComputeDivergence_kernel<Minkowski> (src/kernels/
+ * divergences.hpp:23-135) writes E1(i) - E1(i-1) + E2(j) - E2(j-1)
+ * [+ E3(k) - E3(k-1)] into component `comp` of bckp (EB layout) at the
+ * active cells; EB's lower ghosts must be filled. */
+int pic_output_divergence(pic_ctx* ctx, const void* EB, void* bckp, int32_t comp, void* stream);
+
+/* PrepareOutput flags (src/global/enums.h) */
+#define PIC_OUT_INTERP_EDGES 1u /* E, J: cell centre from the edges */
+#define PIC_OUT_INTERP_FACES 2u /* B: cell centre from the faces */
+#define PIC_OUT_TO_HAT 4u       /* ConvertToHat: times dx along the simulated axes */
+
+/* The field output of Metadomain::Write (src/framework/domain/
+ * metadomain_io.cpp:380-700) for one quantity, in one pass:
+ * DeepCopyFields, FieldsToPhys_kernel<Minkowski> (src/kernels/
+ * fields_to_phys.hpp:33-241) and the writer's downsampling
+ * (src/output/writer.cpp:199-300, first cell 0). Reads components
+ * c0 .. c0 + ncomp - 1 (ncomp 1 or 3) of `src` (EB layout if is_em, else the
+ * current layout) and writes out[c][o3][o2][o1] (o1 fastest), o_d over
+ * ceil(n_d / dwn[d]) output cells taking cell o_d * dwn[d]. With ncomp = 1
+ * (a moment) the values are copied as they are (flags must be 0). The
+ * interpolation reads the first ghost layer above the active range: fill the
+ * ghosts first. */
+int pic_output_field(pic_ctx* ctx, const void* src, int32_t is_em, int32_t c0, int32_t ncomp,
+                     uint32_t flags, double dx, const int32_t dwn[3], void* out, void* stream);
+
+/* Particles::OutputWrite without tracking (src/framework/containers/
+ * particles_io.cpp:93-235) with PrtlToPhys_kernel<SRPIC, Minkowski, false>
+ * (src/kernels/prtls_to_phys.hpp:28-218): *nout = npart / stride records, the
+ * p-th from particle p * stride, dead ones included as there:
+ * x_d = (i_d + dx_d) * dx + xmin[d] for the simulated axes, u and the weight
+ * copied. Output arrays are real_t, device-resident, caller-allocated with
+ * room for npart / stride records. */
+int pic_output_particles(pic_ctx* ctx, const pic_species* sp, int64_t stride, double dx,
+                         const double xmin[3], void* const x_out[3], void* const u_out[3],
+                         void* w_out, int64_t* nout, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,6 +1,6 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles oracle/srpic_oracle.c, grpic_oracle.c and inject_oracle.c twice with gcc into
+Compiles oracle/srpic_oracle.c, grpic_oracle.c, inject_oracle.c and output_oracle.c twice with gcc into
 oracle/_build/:
   liboracle_f32.so  (real = float,  the reference's SINGLE_PRECISION build)
   liboracle_f64.so  (real = double)
@@ -14,7 +14,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
 
-SOURCES = ["srpic_oracle.c", "grpic_oracle.c", "inject_oracle.c"]
+SOURCES = ["srpic_oracle.c", "grpic_oracle.c", "inject_oracle.c", "output_oracle.c"]
 FLAGS = ["-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
          "-fopenmp", "-Wall", "-Wno-unused-function"]
 
@@ -30,7 +30,7 @@ def build(verbose=False):
     os.makedirs(OUT, exist_ok=True)
     deps = [os.path.join(HERE, s) for s in SOURCES] + [
         os.path.join(HERE, h) for h in ("srpic_oracle.h", "grpic_oracle.h", "grpic_metric.inc",
-                                        "inject_oracle.h")]
+                                        "inject_oracle.h", "output_oracle.h")]
     libs = {}
     for tag, defs in (("f32", ["-DORC_SINGLE"]), ("f64", [])):
         target = os.path.join(OUT, f"liboracle_{tag}.so")

@@ -108,6 +108,17 @@ def lib(real):
         L.orc_inject_count.argtypes = [C.c_int, P]
         L.orc_inject_uniform.restype = C.c_int64
         L.orc_inject_uniform.argtypes = [G, S, S, P, C.POINTER(C.c_int64)]
+        I, D_ = C.c_int, C.c_double
+        L.orc_output_moment.argtypes = [G, S, I, I, I, I, I, I, D_, D_, V, I]
+        L.orc_spline.restype = C.c_double
+        L.orc_spline.argtypes = [I, D_]
+        L.orc_sync_moments.argtypes = [G, V, I, I]
+        L.orc_output_divergence.argtypes = [G, V, V, I]
+        L.orc_normalize_by_rho.argtypes = [G, V, I, I, I, I]
+        L.orc_output_field.argtypes = [G, V, I, I, I, C.c_uint, D_, C.POINTER(C.c_int), V]
+        L.orc_output_particles.restype = C.c_int64
+        L.orc_output_particles.argtypes = [G, S, C.c_int64, D_, C.POINTER(C.c_double), V, V, V,
+                                           V, V, V, V]
         _libs[tag] = L
     return _libs[tag]
 
@@ -253,6 +264,40 @@ class Oracle:
             s = self.species(sp)
             self.L.orc_particle_moments(C.byref(s), out)
         return list(out)
+
+    # output preparation (output_oracle.c)
+    def output_moment(self, species, mom, bckp, comp):
+        """mom: dict(id, c1, c2, order, smoothing, use_weights, inv_n0, dx)."""
+        for sp in species:
+            s = self.species(sp)
+            self.L.orc_output_moment(C.byref(self.og), C.byref(s), mom["id"], mom.get("c1", 0),
+                                     mom.get("c2", 0), mom.get("order", 0),
+                                     mom.get("smoothing", 2), int(mom.get("use_weights", 0)),
+                                     float(mom["inv_n0"]), float(mom["dx"]), _p(bckp), comp)
+
+    def spline(self, order, x):
+        return self.L.orc_spline(order, x)
+
+    def output_divergence(self, EB, bckp, comp):
+        self.L.orc_output_divergence(C.byref(self.og), _p(EB), _p(bckp), comp)
+
+    def sync_moments(self, bckp, c0, c1):
+        self.L.orc_sync_moments(C.byref(self.og), _p(bckp), c0, c1)
+
+    def normalize_by_rho(self, bckp, c_rho, cv):
+        self.L.orc_normalize_by_rho(C.byref(self.og), _p(bckp), c_rho, cv[0], cv[1], cv[2])
+
+    def output_field(self, src, is_em, c0, ncomp, flags, dx, dwn, out):
+        d = (C.c_int * 3)(*[int(x) for x in (list(dwn) + [1, 1, 1])[:3]])
+        self.L.orc_output_field(C.byref(self.og), _p(src), int(is_em), c0, ncomp, flags, dx, d,
+                                _p(out))
+
+    def output_particles(self, sp, stride, dx, xmin, x, u, w):
+        s = self.species(sp)
+        xm = (C.c_double * 3)(*[float(v) for v in (list(xmin) + [0.0, 0.0, 0.0])[:3]])
+        xs = [(_p(x[d]) if d < len(x) else None) for d in range(3)]
+        return self.L.orc_output_particles(C.byref(self.og), C.byref(s), int(stride), float(dx),
+                                           xm, *xs, _p(u[0]), _p(u[1]), _p(u[2]), _p(w))
 
     # the SR step sequence of SRPICEngine::step_forward (srpic.hpp:65-188)
     def step(self, species, EB, J, buff, prm, step, filter_passes=None):
