@@ -221,7 +221,7 @@ def precision_twin(w, n, steps, sort_interval, every, timers=False, warm=0):
     of the FP32 run against the FP64 run and both throughputs."""
     import dataclasses
     from entity_gb300.inputs import empty_field
-    from entity_gb300.sim import Context
+    from entity_gb300.sim import Context, HostPipe
     g32, EB32, J32, buff32, sp32 = make_setup(w, "cuda", n=n)
     g64 = dataclasses.replace(g32, real=torch.float64)
     EB64 = EB32.double()
@@ -312,7 +312,7 @@ def run_ours(args, w):
     from __graft_entry__ import build
     build()
     from entity_gb300 import abi
-    from entity_gb300.sim import Context
+    from entity_gb300.sim import Context, HostPipe
     lib = abi.load()
 
     g, EB, J, buff, sp = make_setup(w, "cuda", n=args.cells)
@@ -361,17 +361,21 @@ def run_ours(args, w):
     if args.workload in DRAM_BYTES_PER_PARTICLE and not args.reference_sort_key:
         traffic = DRAM_BYTES_PER_PARTICLE[args.workload] * npart
 
-    # end to end through pic_srpic_step with host buffers: every step copies
-    # the full particle and field state from pinned host memory and back
+    # end to end through pic_srpic_step_host with host buffers: every step
+    # copies the state in from pinned host memory (EB and each species' i, dx,
+    # u, w, tag) and the result out (the same plus J); the pipe overlaps one
+    # step's outgoing copies with the next step's incoming ones
     e2e = None
     if not args.no_e2e:
-        tensors = [EB, J, buff]
-        for s in sp:
-            tensors += [*s.i[:g.dim], *s.dx[:g.dim], *s.u, s.w, s.tag]
-        host = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in tensors]
-        for h, t in zip(host, tensors):
-            h.copy_(t)
-        nbytes = sum(t.numel() * t.element_size() for t in tensors)
+        from entity_gb300.inputs import SpeciesArrays
+        pin = lambda t: None if t is None else torch.empty(t.shape, dtype=t.dtype,
+                                                           pin_memory=True).copy_(t)
+        hsp = [SpeciesArrays([pin(x) for x in s.i], [pin(x) for x in s.dx],
+                             [None] * len(s.i_prev), [None] * len(s.dx_prev),
+                             [pin(x) for x in s.u], pin(s.w), pin(s.tag), s.mass, s.charge,
+                             s.pusher, s.npart, s.index) for s in sp]
+        hEB, hJ = pin(EB), pin(J)
+        pipe = HostPipe()
         k2 = max(1, min(args.steps, args.e2e_steps))
         torch.cuda.synchronize()
         barrier()
@@ -379,18 +383,18 @@ def run_ours(args, w):
         t0 = time.perf_counter()
         a0.record()
         for k in range(k2):
-            for h, t in zip(host, tensors):
-                t.copy_(h, non_blocking=True)
-            ctx.step(sp, EB, J, buff, prm, args.warmup + args.steps + k)
-            for h, t in zip(host, tensors):
-                h.copy_(t, non_blocking=True)
+            ctx.step_host(pipe, hsp, sp, hEB, EB, hJ, J, buff, prm, args.warmup + args.steps + k)
+        pipe.sync()
         a1.record()
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+        nin, nout = pipe.bytes()
+        pipe.close()
         barrier()
         te, _ = reduce_over_ranks(max(a0.elapsed_time(a1) / 1e3, 1e-9), 0, world, "cuda")
-        e2e = {"value": tot_part * k2 / te, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-               "d2h_bytes_per_step": nbytes, "steps": k2, "wall_s": wall}
+        e2e = {"value": tot_part * k2 / te, "unit": UNIT, "h2d_bytes_per_step": nin,
+               "d2h_bytes_per_step": nout, "steps": k2, "wall_s": wall,
+               "api": "pic_srpic_step_host"}
 
     if rank != 0:
         return
@@ -439,7 +443,7 @@ def run_adjoint(args, w):
     build()
     from entity_gb300 import abi
     from entity_gb300 import adjoint as A
-    from entity_gb300.sim import Context
+    from entity_gb300.sim import Context, HostPipe
     lib = abi.load()
     nsteps = args.adjoint_steps or w["steps"]
     every = args.checkpoint_every or w["every"]
@@ -713,7 +717,7 @@ def main():
                     help="sort by the reference's i1-major cell key (untiled push/deposit)")
     ap.add_argument("--cells", type=int, nargs="+", default=None,
                     help="override the grid (smaller cases for profiling)")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -63,9 +63,11 @@ extern "C" int pic_srpic_gradient(pic_ctx* ctx, pic_species* sp, pic_species_adj
   p.write_prev      = 0;
   const int64_t nseg = (nsteps + every - 1) / every;
   if (nseg + every > (int64_t)1 << 30) return PIC_ERR_UNSUPPORTED;
-#define PIC_TRY(x)              \
-  if ((st = (x)) != PIC_OK) \
-    return st;
+#define PIC_TRY(x)            \
+  do {                        \
+    if ((st = (x)) != PIC_OK) \
+      return st;              \
+  } while (0)
   // forward with checkpoints; the steps of the last segment keep their
   // starting states as they go, so that segment needs no recompute
   const int64_t last0 = (nseg - 1) * every;

@@ -18,9 +18,11 @@ int gr_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, int32_t nsp, 
             const pic_step_params& p, const pic_gr_params& gp, int64_t step, void* stream,
             size_t em_bytes) {
   int st;
-#define PIC_TRY(x)          \
-  if ((st = (x)) != PIC_OK) \
-    return st;
+#define PIC_TRY(x)            \
+  do {                        \
+    if ((st = (x)) != PIC_OK) \
+      return st;              \
+  } while (0)
   auto mark = [&](int phase, int end) { return pic_timer_mark(ctx, phase, end, stream); };
   // gr_bc::main boundaries act on both em and em0 (grpic/fields_bcs.h:220-262)
   // the directions in Directions<2>::orth order: horizon (-x1), axis (-x2,

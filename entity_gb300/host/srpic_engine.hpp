@@ -103,9 +103,11 @@ inline int SortParticles(Domain& dom, const pic_step_params& p, int64_t step, vo
 template <typename real>
 int StepForward(Domain& dom, const pic_step_params& p, int64_t step, void* stream) {
   int st;
-#define PIC_TRY(x)          \
-  if ((st = (x)) != PIC_OK) \
-    return st;
+#define PIC_TRY(x)            \
+  do {                        \
+    if ((st = (x)) != PIC_OK) \
+      return st;              \
+  } while (0)
   // timer::Timers phases (srpic.hpp:85-187); no-ops unless timers are enabled
   auto mark = [&](int phase, int end) { return pic_timer_mark(dom.ctx, phase, end, stream); };
   PIC_TRY(mark(PIC_PHASE_STEP, 0));

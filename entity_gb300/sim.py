@@ -84,6 +84,36 @@ def make_species(sp: SpeciesArrays, dim: int) -> abi.PicSpecies:
     return ps
 
 
+class HostPipe:
+    """pic_host_pipe: the copy streams of a domain whose state lives in pinned
+    host memory (Context.step_host)."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        abi.call("pic_host_pipe_create", C.byref(h))
+        self.h = h
+
+    def sync(self):
+        abi.call("pic_host_pipe_sync", self.h)
+
+    def bytes(self):
+        """(host-to-device, device-to-host) bytes of the last step."""
+        a, b = C.c_int64(0), C.c_int64(0)
+        abi.call("pic_host_pipe_bytes", self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def close(self):
+        if self.h:
+            abi.call("pic_host_pipe_destroy", self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Context:
     """One domain's context (pic_create / pic_destroy)."""
 
@@ -265,6 +295,22 @@ class Context:
         for k, s in enumerate(species):
             s.npart = arr[k].npart
         return loss.value
+
+    def step_host(self, pipe: HostPipe, host_species, dev_species, hEB, dEB, hJ, dJ, buff,
+                  prm: abi.PicStepParams, step, stream=None):
+        """pic_srpic_step_host: host_species / hEB / hJ are pinned CPU tensors,
+        dev_species / dEB / dJ their device mirrors. Asynchronous: the host
+        arrays hold the result after pipe.sync()."""
+        hs = (abi.PicSpecies * len(host_species))(
+            *[make_species(s, self.g.dim) for s in host_species])
+        ds = (abi.PicSpecies * len(dev_species))(
+            *[make_species(s, self.g.dim) for s in dev_species])
+        abi.call("pic_srpic_step_host", self.h, pipe.h, hs, ds, len(dev_species), _ptr(hEB),
+                 _ptr(dEB), _ptr(hJ), _ptr(dJ), _ptr(buff), C.byref(prm), int(step),
+                 _stream_ptr(stream))
+        for k in range(len(dev_species)):
+            host_species[k].npart = hs[k].npart
+            dev_species[k].npart = ds[k].npart
 
     def step_adjoint(self, species, adjoints, EB, lamEB, prm: abi.PicStepParams, stream=None):
         arr = (abi.PicSpecies * len(species))(*[make_species(s, self.g.dim) for s in species])

@@ -302,6 +302,33 @@ typedef struct {
 int pic_srpic_step(pic_ctx* ctx, pic_species* sp, int32_t nspecies, void* EB, void* J,
                    void* buff, const pic_step_params* prm, int64_t step, void* stream);
 
+/* A domain whose state lives in pinned host memory, as the reference's OpenMP
+ * build keeps its Views on the host (the caller of this path then passes host
+ * buffers). The pipe holds two copy streams and per-array events; create one
+ * per domain. No reference counterpart. */
+typedef struct pic_host_pipe pic_host_pipe;
+int pic_host_pipe_create(pic_host_pipe** out);
+int pic_host_pipe_destroy(pic_host_pipe* pipe);
+/* Waits for every copy the pipe has queued; the host arrays then hold the
+ * last step's result. */
+int pic_host_pipe_sync(pic_host_pipe* pipe);
+/* Bytes the last pic_srpic_step_host call copied host to device and back. */
+int pic_host_pipe_bytes(const pic_host_pipe* pipe, int64_t* bytes_in, int64_t* bytes_out);
+
+/* One pic_srpic_step with host arrays as source and sink: hsp[k] (pinned host)
+ * and dsp[k] (device) describe the same species, with equal npart; hEB / dEB
+ * and hJ / dJ likewise, buff is device scratch. Copied in: EB and each
+ * species' i, dx, u, weight and tag (the prev arrays stay on the device, as
+ * the step rewrites them before reading). Copied out: J, EB and the same
+ * species arrays, with npart updated in both descriptions. Each array's
+ * input copy waits only for the previous call's output copy of that array,
+ * so one step's device-to-host copies overlap the next step's host-to-device
+ * copies. Asynchronous: the host arrays hold the result after
+ * pic_host_pipe_sync, and the device mirrors belong to the pipe until then. */
+int pic_srpic_step_host(pic_ctx* ctx, pic_host_pipe* pipe, pic_species* hsp, pic_species* dsp,
+                        int32_t nspecies, void* hEB, void* dEB, void* hJ, void* dJ, void* buff,
+                        const pic_step_params* prm, int64_t step, void* stream);
+
 /* ------------------------------------------------------------------------
  * Adjoint (reverse mode) of the SR step. No counterpart in the reference.
  *
