@@ -144,6 +144,11 @@ SIGNATURES = {
                               C.c_double, _VP]),
     "pic_push_deposit": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32, _VP, _VP, C.c_double,
                                    C.c_double, C.c_double, C.c_uint32, _VP]),
+    "pic_tile_offsets": (C.c_int, [_VP, C.POINTER(PicSpecies), C.POINTER(C.c_int32), C.c_int64,
+                                   C.POINTER(C.c_int64), _VP]),
+    "pic_push_deposit_tiles": (C.c_int, [_VP, C.POINTER(PicSpecies), _VP, _VP, C.c_double,
+                                         C.c_double, C.c_double, C.c_int64, C.c_int64, C.c_uint32,
+                                         _VP]),
     "pic_sync_currents": (C.c_int, [_VP, _VP, _VP, _VP]),
     "pic_filter_currents": (C.c_int, [_VP, _VP, _VP, C.c_int32, _VP]),
     "pic_fill_ghosts": (C.c_int, [_VP, _VP, C.c_int32, C.c_int32, C.c_int32, _VP]),

@@ -176,7 +176,8 @@ pic_species species_tail(const pic_species& sp, int64_t first, int real_bytes) {
 
 template <typename real>
 int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void* EB, void* J,
-              double dt, double omegaB0, double dx, bool write_prev, cudaStream_t s) {
+              double dt, double omegaB0, double dx, bool write_prev, cudaStream_t s,
+              int64_t tile0 = 0, int64_t tile1 = -1) {
   pic::TiledArgs<real> a;
   a.nsp = (int)sps.size();
   for (int k = 0; k < a.nsp; ++k) {
@@ -194,6 +195,9 @@ int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void
   }
   int ts[3];
   ntiles_of(c, a.ntiles, ts);
+  const int64_t nt_all = (int64_t)a.ntiles[0] * a.ntiles[1] * a.ntiles[2];
+  a.tile0 = (int)tile0;
+  a.tile1 = (int)(tile1 < 0 ? nt_all : tile1);
   for (int d = 0; d < 3; ++d) {
     a.pc.n[d]     = c->grid.n[d];
     a.pc.bc[d][0] = c->grid.prtl_bc[d][0];
@@ -583,6 +587,50 @@ int pic_push_deposit(pic_ctx* c, const pic_species* sp, int32_t nspecies, const 
     if (st != PIC_OK) return st;
   }
   return PIC_OK;
+}
+
+int pic_tile_offsets(pic_ctx* c, const pic_species* sp, int32_t* out, int64_t cap,
+                     int64_t* ntiles, void* stream) {
+  if (!c || !sp || !ntiles) return PIC_ERR_ARG;
+  int nt[3], ts[3];
+  ntiles_of(c, nt, ts);
+  *ntiles                = (int64_t)nt[0] * nt[1] * nt[2];
+  const SpeciesBins* b   = find_bins(c, sp->index, false);
+  if (!b || !b->valid || b->npart != sp->npart || !b->tile_start) return PIC_ERR_UNSUPPORTED;
+  if (!out) return PIC_OK;
+  if (cap < *ntiles + 1) return PIC_ERR_ARG;
+  cudaStream_t s = strm(stream);
+  if (cudaMemcpyAsync(out, b->tile_start, sizeof(int32_t) * (size_t)(*ntiles + 1),
+                      cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
+int pic_push_deposit_tiles(pic_ctx* c, const pic_species* sp, const void* EB, void* J, double dt,
+                           double omegaB0, double dx, int64_t tile_lo, int64_t tile_hi,
+                           uint32_t flags, void* stream) {
+  if (!c || !sp || !EB || !J) return PIC_ERR_ARG;
+  const bool write_prev = (flags & PIC_PD_WRITE_PREV) != 0;
+  int        st         = validate_species(c, sp, write_prev);
+  if (st != PIC_OK) return st;
+  if (sp->pusher != PIC_PUSHER_BORIS && sp->pusher != PIC_PUSHER_VAY) return PIC_ERR_UNSUPPORTED;
+  if (sp->mass == 0.0f) return PIC_ERR_ARG;
+  int nt[3], ts[3];
+  ntiles_of(c, nt, ts);
+  const int64_t      nt_all = (int64_t)nt[0] * nt[1] * nt[2];
+  const SpeciesBins* b      = find_bins(c, sp->index, false);
+  if (!b || !b->valid || b->npart != sp->npart) return PIC_ERR_UNSUPPORTED;
+  if (tile_lo < 0 || tile_hi > nt_all || tile_lo > tile_hi) return PIC_ERR_ARG;
+  if (!(flags & PIC_PD_NO_ZERO)) {
+    st = is_f64(c) ? zero_J<double>(c, J, strm(stream)) : zero_J<float>(c, J, strm(stream));
+    if (st != PIC_OK) return st;
+  }
+  if (tile_lo == tile_hi || sp->npart == 0) return PIC_OK;
+  const std::vector<const pic_species*> one{ sp };
+  return is_f64(c) ? run_tiled<double>(c, one, EB, J, dt, omegaB0, dx, write_prev, strm(stream),
+                                       tile_lo, tile_hi)
+                   : run_tiled<float>(c, one, EB, J, dt, omegaB0, dx, write_prev, strm(stream),
+                                      tile_lo, tile_hi);
 }
 
 int pic_sync_currents(pic_ctx* c, void* J, void* buff, void* stream) {

@@ -153,6 +153,7 @@ struct TiledArgs {
   PushConsts         pc;
   int                periodic[3];
   int                ntiles[3];
+  int                tile0, tile1;  // linear tiles [tile0, tile1) of this launch
   FieldView<real>    EB;
   FieldView<real>    J;
   real               dt, dx, inv_dt;
@@ -207,7 +208,7 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
   real*          Jr  = reinterpret_cast<real*>(Jw);  // real_t accumulation of dense tiles
   __shared__ unsigned int s_qmax;  // bit pattern of the tile's largest |q w| max(1/dt, 1)
 
-  const int t  = blockIdx.x;
+  const int t  = blockIdx.x + a.tile0;
   const int tx = t % a.ntiles[0];
   const int ty = (t / a.ntiles[0]) % a.ntiles[1];
   const int tz = D == 3 ? t / (a.ntiles[0] * a.ntiles[1]) : 0;

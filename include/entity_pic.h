@@ -179,6 +179,28 @@ int pic_push_deposit(pic_ctx* ctx, const pic_species* sp, int32_t nspecies, cons
                      void* J, double dt, double omegaB0, double dx, uint32_t flags,
                      void* stream);
 
+/* The tile offsets of a species binned by PIC_SORT_TILED: out[t] is the first
+ * particle of tile t (tiles in the sort's linear order, out[ntiles] = the
+ * alive count; dead particles follow). *ntiles is always set; with
+ * out == NULL only the count is returned. PIC_ERR_UNSUPPORTED when the
+ * species has no valid binning (not sorted with PIC_SORT_TILED since its
+ * npart last changed). Synchronises the stream. No reference counterpart. */
+int pic_tile_offsets(pic_ctx* ctx, const pic_species* sp, int32_t* out, int64_t cap,
+                     int64_t* ntiles, void* stream);
+
+/* pic_push_deposit for the particles of tiles [tile_lo, tile_hi) of one
+ * binned species (Boris or Vay): the tiled kernel over those tiles, then the
+ * per-particle kernel over the ones it deferred. J is zeroed first unless
+ * PIC_PD_NO_ZERO. Covering every tile once, in any number of calls, gives the
+ * same particles and the same J (up to the order of the J additions) as one
+ * pic_push_deposit call. Dead particles after the alive prefix are not
+ * visited. PIC_ERR_UNSUPPORTED without a valid binning. No reference
+ * counterpart: it lets a caller push part of a species while the rest is
+ * still being copied in. */
+int pic_push_deposit_tiles(pic_ctx* ctx, const pic_species* sp, const void* EB, void* J,
+                           double dt, double omegaB0, double dx, int64_t tile_lo,
+                           int64_t tile_hi, uint32_t flags, void* stream);
+
 /* Metadomain::SynchronizeFields(Comm::J) + CommunicateFields(Comm::J)
  * (metadomain_comm.cpp:408-562, 204-367): periodic ghost currents are added
  * to their active images, then ghosts are refilled. buff is unused (kept for

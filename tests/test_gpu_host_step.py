@@ -29,12 +29,17 @@ def _pinned(sp):
                          sp.pusher, sp.npart, sp.index)
 
 
-@pytest.mark.parametrize("dim", [2, 3])
-def test_host_resident_steps_match_device_steps(dim):
+@pytest.mark.parametrize("dim,sort_tiled,clear,deposit", [
+    (2, False, 100, True), (3, False, 100, True), (2, True, 100, True), (3, True, 3, True),
+    (2, True, 100, False)])
+def test_host_resident_steps_match_device_steps(dim, sort_tiled, clear, deposit):
+    """Tiled sorts split each species into tile groups that are copied and
+    pushed one by one; dead removal changes the counts and the groups."""
     n = (32, 24, 1) if dim == 2 else (16, 16, 8)
     g = GridSpec(dim=dim, n=n, order=2, real=torch.float64)
     prm = step_params(g, cfl=0.45, ppc0=8.0, skindepth0=4.0, larmor0=3.0, nfilter=2,
-                      sort_interval=2, write_prev=True)
+                      sort_interval=2, clear_interval=clear, write_prev=True,
+                      sort_tiled=sort_tiled, deposit=deposit)
     sps = [make_species(g, 4, 0.2, 0.3, 31, charge=-1.0),
            make_species(g, 4, 0.2, -0.3, 32, charge=1.0, index=2)]
     for s in sps:   # a few dead particles for the sort's dead removal
@@ -44,7 +49,8 @@ def test_host_resident_steps_match_device_steps(dim):
     ctx = Context(g)
     da = [s.clone().to("cuda") for s in sps]
     EBa, Ja, Ba = EB0.cuda(), empty_field(g, 3, "cuda"), empty_field(g, 3, "cuda")
-    for k in range(5):
+    nsteps = 9
+    for k in range(nsteps):
         ctx.step(da, EBa, Ja, Ba, prm, k)
     # host-resident: the state lives in pinned memory; the device arrays are
     # mirrors that start out as garbage
@@ -58,7 +64,7 @@ def test_host_resident_steps_match_device_steps(dim):
     EBb = torch.full_like(EBa, 7.0)
     Jb, Bb = empty_field(g, 3, "cuda"), empty_field(g, 3, "cuda")
     pipe = HostPipe()
-    for k in range(5):
+    for k in range(nsteps):
         ctx2.step_host(pipe, hs, ds, hEB, EBb, hJ, Jb, Bb, prm, k)
     pipe.sync()
     torch.cuda.synchronize()
@@ -81,4 +87,6 @@ def test_host_resident_steps_match_device_steps(dim):
         assert torch.equal(h.tag[:m], a.tag[:m].cpu())
         want_in += m * (dim * 8 + 4 * rb + 2)
     assert nin == want_in
-    assert nout == want_in + hJ.numel() * rb
+    assert nout == want_in + (hJ.numel() * rb if deposit else 0)
+    if clear == 3:
+        assert all(h.npart < s.npart for h, s in zip(hs, sps))  # the dead were removed
