@@ -15,7 +15,9 @@
 //     waits only for its own output copy. So one step's outgoing traffic
 //     overlaps the next step's incoming traffic, and the host link runs in
 //     both directions at once.
-//   - Fields and particles use separate copy streams in each direction.
+//   - Fields and particles use separate streams in each direction, and the
+//     fields are copied by a kernel through the mapped host pointer, so that
+//     they never queue behind the particle groups on the copy engines.
 // The call returns once everything is queued: the host arrays hold the result
 // after pic_host_pipe_sync, and the device mirrors belong to the pipe until
 // then.
@@ -26,6 +28,10 @@
 
 #include "../../include/entity_pic.h"
 #include "srpic_engine.hpp"
+
+namespace pic {
+void note_launch();  // the library's kernel launch counter
+}
 
 namespace {
 constexpr int kChunks = 4;  // tile groups per binned species
@@ -133,6 +139,48 @@ int make_split(pic_ctx* ctx, const pic_species& sp, cudaStream_t s, Split& out) 
   out.tile = { 0, 0 };
   out.part = { 0, sp.npart };
   return PIC_OK;
+}
+
+// SM-driven copy between device memory and mapped pinned host memory. The
+// fields travel this way: the copy engines serve their queue in submission
+// order, so the fields' copies at the end of a step would otherwise wait
+// behind every particle group queued earlier in the step.
+__global__ void k_copy_bytes(const unsigned char* __restrict__ src,
+                             unsigned char* __restrict__ dst, size_t bytes) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t t0     = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const bool   vec    = ((((uintptr_t)src) | ((uintptr_t)dst)) & 15u) == 0;
+  size_t       head   = 0;
+  if (vec) {
+    const size_t n16 = bytes / 16;
+    const uint4* s4  = (const uint4*)src;
+    uint4*       d4  = (uint4*)dst;
+    for (size_t i = t0; i < n16; i += stride) d4[i] = s4[i];
+    head = n16 * 16;
+  }
+  for (size_t i = head + t0; i < bytes; i += stride) dst[i] = src[i];
+}
+
+// the device address of a pinned host buffer, or nullptr when the device
+// cannot address it directly
+void* mapped(void* host) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+cudaError_t copy_field(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind,
+                       cudaStream_t q) {
+  void* hd = mapped(kind == cudaMemcpyHostToDevice ? const_cast<void*>(src) : dst);
+  if (!hd || bytes == 0) return bytes ? cudaMemcpyAsync(dst, src, bytes, kind, q) : cudaSuccess;
+  const unsigned char* s = (const unsigned char*)(kind == cudaMemcpyHostToDevice ? hd : src);
+  unsigned char*       d = (unsigned char*)(kind == cudaMemcpyHostToDevice ? dst : hd);
+  k_copy_bytes<<<152 * 4, 256, 0, q>>>(s, d, bytes);
+  pic::note_launch();
+  return cudaGetLastError();
 }
 
 int remake_events(std::vector<cudaEvent_t>& v, size_t n) {
@@ -273,9 +321,12 @@ int pic_srpic_step_host(pic_ctx* ctx, pic_host_pipe* p, pic_species* hsp, pic_sp
   auto copy_out = [&](size_t a0, size_t a1, int64_t& bytes) {
     for (size_t a = a0; a < a1; ++a) {
       cudaStream_t q = a < 2 ? p->down_f : p->down;
-      if (slots[a].bytes > 0 && cudaMemcpyAsync(slots[a].host, slots[a].dev, slots[a].bytes,
-                                                cudaMemcpyDeviceToHost, q) != cudaSuccess)
-        return false;
+      const cudaError_t e =
+        a < 2 ? copy_field(slots[a].host, slots[a].dev, slots[a].bytes, cudaMemcpyDeviceToHost, q)
+        : slots[a].bytes > 0
+          ? cudaMemcpyAsync(slots[a].host, slots[a].dev, slots[a].bytes, cudaMemcpyDeviceToHost, q)
+          : cudaSuccess;
+      if (e != cudaSuccess) return false;
       bytes += (int64_t)slots[a].bytes;
       if (cudaEventRecord(p->out_done[a], q) != cudaSuccess) return false;
       p->pending[a] = 1;
@@ -303,7 +354,9 @@ int pic_srpic_step_host(pic_ctx* ctx, pic_host_pipe* p, pic_species* hsp, pic_sp
   for (size_t a = 1; a < slots.size(); ++a) {
     cudaStream_t q = a < 2 ? p->up_f : p->up;
     if (!wait_out(q, a)) return PIC_ERR_CUDA;
-    if (slots[a].bytes > 0)
+    if (a < 2)
+      PIC_CU(copy_field(slots[a].dev, slots[a].host, slots[a].bytes, cudaMemcpyHostToDevice, q));
+    else if (slots[a].bytes > 0)
       PIC_CU(cudaMemcpyAsync(slots[a].dev, slots[a].host, slots[a].bytes, cudaMemcpyHostToDevice,
                              q));
     bin += (int64_t)slots[a].bytes;
