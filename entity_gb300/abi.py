@@ -37,6 +37,7 @@ PIC_SORT_REMOVE_DEAD = 1
 PIC_SORT_SKIP_PREV = 2
 PIC_SORT_SPATIAL = 4
 PIC_SORT_TILED = 8
+PIC_SORT_NO_SYNC = 16
 
 
 class PicGrid(C.Structure):

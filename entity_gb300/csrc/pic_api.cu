@@ -750,6 +750,8 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
   if (st != PIC_OK) return st;
   const bool remove_dead = (flags & PIC_SORT_REMOVE_DEAD) != 0;
   const bool spatial     = (flags & PIC_SORT_SPATIAL) != 0;
+  const bool no_sync     = (flags & PIC_SORT_NO_SYNC) != 0;
+  if (no_sync && remove_dead) return PIC_ERR_ARG;
   cudaStream_t  s        = strm(stream);
   const int64_t np       = sp->npart;
   if (npart_out) *npart_out = np;
@@ -872,6 +874,18 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
         return PIC_ERR_NOMEM;
       b->ovf_cap = cap;
     }
+  }
+  if (no_sync) {
+    // npart is unchanged; the dead sit after tile_start[ntiles] and are never
+    // pushed, so the binned range may cover the whole species
+    if (tiled) {
+      SpeciesBins* b = find_bins(c, sp->index, true);
+      b->nalive = np;
+      b->npart  = np;
+      b->valid  = true;
+    }
+    if (npart_out) *npart_out = np;
+    return PIC_OK;
   }
   // the one synchronisation of a sort: the dead count and the error word
   int32_t            n_dead = 0;

@@ -91,6 +91,8 @@ inline int SortParticles(Domain& dom, const pic_step_params& p, int64_t step, vo
     }
     if (!flags) continue;
     if (!p.write_prev) flags |= PIC_SORT_SKIP_PREV;
+    // a spatial sort leaves npart as it is: no need to wait for it
+    if (!(flags & PIC_SORT_REMOVE_DEAD)) flags |= PIC_SORT_NO_SYNC;
     int64_t    n  = s.npart;
     const int  st = pic_sort(dom.ctx, &s, flags, &n, stream);
     if (st != PIC_OK) return st;

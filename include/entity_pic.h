@@ -70,6 +70,12 @@ extern "C" {
  * the reference's key only sets a traversal order, and this one lets a tile's
  * particles be read as one contiguous range. */
 #define PIC_SORT_TILED 8u
+/* Without PIC_SORT_REMOVE_DEAD: return without waiting for the sort (npart
+ * cannot change). Out-of-grid particles are then only counted in the error
+ * word (out[1]) instead of also failing the call with PIC_ERR_DEVICE. With
+ * PIC_SORT_REMOVE_DEAD it is PIC_ERR_ARG: the new count needs the wait. No
+ * reference counterpart. */
+#define PIC_SORT_NO_SYNC 16u
 
 /* Grid and build choices of a domain (Grid/Mesh, src/framework/domain/grid.h;
  * N_GHOSTS and SHAPE_ORDER, src/global/global.h:130-136). Field element

@@ -114,3 +114,37 @@ def test_counts_beyond_32_bit_indices_are_refused():
     ctx.push(sp, EB, 0.3, 1.0, g.dx)
     torch.cuda.synchronize()
     assert ctx.device_errors() == [0, 0, 0, 0]
+
+
+def test_sort_without_waiting_matches_the_waiting_sort():
+    """PIC_SORT_NO_SYNC: same order as the waiting sort, no dead removal
+    allowed, out-of-grid particles only counted in the error word; the tiled
+    push that follows gives the same particles and J."""
+    g = GridSpec(dim=3, n=(16, 12, 8), order=2, real=torch.float32)
+    base = make_species(g, 3, 0.2, 0.1, 17, device="cpu", with_prev=False)
+    base.tag[::13] = 0
+    ca, cb = Context(g), Context(g)
+    a, b = base.to("cuda"), base.to("cuda")
+    fl = abi.PIC_SORT_SPATIAL | abi.PIC_SORT_TILED | abi.PIC_SORT_SKIP_PREV
+    assert ca.sort(a, fl) == abi.PIC_OK
+    assert cb.sort(b, fl | abi.PIC_SORT_NO_SYNC) == abi.PIC_OK
+    torch.cuda.synchronize()
+    _assert_particles_equal(a.to("cpu"), b, 3, prev=False)
+    EB = random_fields(g, 4, amp=0.05).cuda()
+    Ja, Jb = empty_field(g, 3, "cuda"), empty_field(g, 3, "cuda")
+    ca.push_deposit([a], EB, Ja, 0.3, 1.0, g.dx)
+    cb.push_deposit([b], EB, Jb, 0.3, 1.0, g.dx)
+    torch.cuda.synchronize()
+    _assert_particles_equal(a.to("cpu"), b, 3, prev=False)
+    # the tile windows' overlapping halos are added with float atomics, in no
+    # fixed order
+    assert float((Ja - Jb).abs().max()) <= 4e-6 * float(Ja.abs().max())
+    n = C.c_int64(0)
+    st = abi.load().pic_sort(cb.h, C.byref(mk(b, 3)),
+                             fl | abi.PIC_SORT_NO_SYNC | abi.PIC_SORT_REMOVE_DEAD, C.byref(n), None)
+    assert st == abi.PIC_ERR_ARG
+    b.i[0][0] = 10_000
+    b.tag[0] = 1
+    assert cb.sort(b, fl | abi.PIC_SORT_NO_SYNC) == abi.PIC_OK
+    torch.cuda.synchronize()
+    assert cb.device_errors(reset=True)[1] == 1
