@@ -90,6 +90,17 @@ BYTES_PER_CELL = 24 + 12
 # fixed particles per cell, so it scales to the full box by npart
 DRAM_BYTES_PER_PARTICLE = {"turb3d": 1104.1e6 / 14155776}
 
+# what binds the dominant kernel beside HBM, from one `ncu --set full` capture
+# of the same kernel on a smaller box of the same plasma: instruction issue
+# and the shared-memory (l1tex) pipe that carries the fixed-point J atomics
+PIPE_LIMITS = {
+    "turb3d": {"issue_active_pct": 58.0, "l1tex_shared_atomic_wavefronts_per_particle": 21.9,
+               "capture": "ncu --set full, one launch on a 96^3 box of the same plasma"},
+    "sweep3d": {"issue_active_pct": 47.2, "l1tex_throughput_pct": 72.2,
+                "l1tex_shared_atomic_wavefronts_per_particle": 81.9,
+                "capture": "ncu --set full, one launch on a 48^3 box of the same plasma"},
+}
+
 
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
@@ -425,6 +436,7 @@ def run_ours(args, w):
                      "kernel": "k_push_deposit_tiled (fused push + deposit, both species, "
                                "plus the overflow-list drain)",
                      "bytes_per_launch": bytes_pd, "launch_ms": pd_ms / pd_n,
+                     "binding_pipes": PIPE_LIMITS.get(args.workload),
                      "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_src})"},
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -692,6 +704,7 @@ def run_sweep(args, w):
                      "frac": achieved / peak, "traffic": None,
                      "kernel": "k_push_deposit_tiled (FP32, both species)",
                      "bytes_per_launch": bytes_pd, "launch_ms": pd_ms / pd_n,
+                     "binding_pipes": PIPE_LIMITS.get("sweep3d"),
                      "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_src})"},
         "precision": pr,
         "cpu_baseline": cpu,
