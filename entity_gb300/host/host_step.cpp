@@ -34,7 +34,7 @@ void note_launch();  // the library's kernel launch counter
 }
 
 namespace {
-constexpr int kChunks = 4;  // tile groups per binned species
+constexpr int kChunks = 8;  // tile groups per binned species
 
 // one species' split: tile ranges and the particle ranges they cover
 struct Split {
