@@ -387,7 +387,7 @@ def run_ours(args, w):
                              s.pusher, s.npart, s.index) for s in sp]
         hEB, hJ = pin(EB), pin(J)
         pipe = HostPipe()
-        k2 = max(1, min(args.steps, args.e2e_steps))
+        k2 = max(1, args.e2e_steps)
         torch.cuda.synchronize()
         barrier()
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -730,7 +730,7 @@ def main():
                     help="sort by the reference's i1-major cell key (untiled push/deposit)")
     ap.add_argument("--cells", type=int, nargs="+", default=None,
                     help="override the grid (smaller cases for profiling)")
-    ap.add_argument("--e2e-steps", type=int, default=8)
+    ap.add_argument("--e2e-steps", type=int, default=16)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

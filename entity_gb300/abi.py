@@ -187,6 +187,7 @@ SIGNATURES = {
     "pic_host_pipe_create": (C.c_int, [C.POINTER(_VP)]),
     "pic_host_pipe_destroy": (C.c_int, [_VP]),
     "pic_host_pipe_sync": (C.c_int, [_VP]),
+    "pic_host_pipe_set_groups": (C.c_int, [_VP, C.c_int32, C.c_int64]),
     "pic_host_pipe_bytes": (C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "pic_srpic_step_host": (C.c_int, [_VP, _VP, C.POINTER(PicSpecies), C.POINTER(PicSpecies),
                                       C.c_int32, _VP, _VP, _VP, _VP, _VP,

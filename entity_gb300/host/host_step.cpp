@@ -7,7 +7,8 @@
 //
 // The copies are pipelined against the compute and against each other:
 //   - A species binned by the tiled sort is cut into up to kChunks groups of
-//     tiles with about equal particle counts. Each group is a contiguous range
+//     tiles with about equal particle counts (at least kMinGroupBytes of
+//     state each). Each group is a contiguous range
 //     of the particle arrays. It is copied in, pushed with
 //     pic_push_deposit_tiles as soon as it has arrived, and (on steps without
 //     a sort) copied out as soon as its push ends.
@@ -34,7 +35,9 @@ void note_launch();  // the library's kernel launch counter
 }
 
 namespace {
-constexpr int kChunks = 8;  // tile groups per binned species
+constexpr int     kChunks        = 8;             // most tile groups per binned species
+constexpr int64_t kMinGroupBytes = 256ll << 20;  // least state per group: fewer, larger
+                                                 // copies for small species
 
 // one species' split: tile ranges and the particle ranges they cover
 struct Split {
@@ -63,6 +66,8 @@ struct pic_host_pipe {
   std::vector<int64_t>     layout;          // range sizes of the previous call
   bool                     any_out = false;
   int64_t                  bytes_in = 0, bytes_out = 0;
+  int                      max_groups      = kChunks;
+  int64_t                  min_group_bytes = kMinGroupBytes;
 };
 
 namespace {
@@ -109,7 +114,8 @@ bool species_ok(const pic_grid& g, const pic_species& h, const pic_species& d) {
 
 // tile groups of a binned species (reading its tile offsets synchronises
 // the stream once), or one group over the whole species
-int make_split(pic_ctx* ctx, const pic_species& sp, cudaStream_t s, Split& out) {
+int make_split(pic_ctx* ctx, const pic_grid& g, const pic_species& sp, int max_groups,
+               int64_t min_bytes, cudaStream_t s, Split& out) {
   out        = Split();
   out.npart  = sp.npart;
   int64_t nt = 0;
@@ -123,9 +129,12 @@ int make_split(pic_ctx* ctx, const pic_species& sp, cudaStream_t s, Split& out) 
     out.tile.push_back(0);
     out.part.push_back(0);
     const int64_t alive = off[(size_t)nt];
-    for (int c = 1; c < kChunks; ++c) {
-      // the first tile that starts at or after c / kChunks of the particles
-      const int64_t target = alive * c / kChunks;
+    const int64_t per   = (int64_t)g.dim * 8 + 4 * (int64_t)g.real_bytes + 2;  // state bytes
+    const int64_t ngrp  = std::max<int64_t>(1, std::min<int64_t>(max_groups,
+                                                               sp.npart * per / min_bytes));
+    for (int64_t c = 1; c < ngrp; ++c) {
+      // the first tile that starts at or after c / ngrp of the particles
+      const int64_t target = alive * c / ngrp;
       const int64_t t = std::lower_bound(off.begin(), off.end(), (int32_t)target) - off.begin();
       if (t > out.tile.back() && t < nt) {
         out.tile.push_back(t);
@@ -246,6 +255,14 @@ int pic_host_pipe_sync(pic_host_pipe* p) {
   return PIC_OK;
 }
 
+int pic_host_pipe_set_groups(pic_host_pipe* p, int32_t max_groups, int64_t min_group_bytes) {
+  if (!p || max_groups < 1 || min_group_bytes < 1) return PIC_ERR_ARG;
+  p->max_groups      = max_groups;
+  p->min_group_bytes = min_group_bytes;
+  for (Split& sp : p->split) sp.npart = -1;  // split anew at the next call
+  return PIC_OK;
+}
+
 int pic_host_pipe_bytes(const pic_host_pipe* p, int64_t* bytes_in, int64_t* bytes_out) {
   if (!p || !bytes_in || !bytes_out) return PIC_ERR_ARG;
   *bytes_in  = p->bytes_in;
@@ -282,7 +299,7 @@ int pic_srpic_step_host(pic_ctx* ctx, pic_host_pipe* p, pic_species* hsp, pic_sp
   p->split.resize((size_t)nspecies);
   for (int k = 0; k < nspecies; ++k)
     if (p->split[k].npart != dsp[k].npart || p->split[k].part.empty())
-      PIC_TRY(make_split(ctx, dsp[k], s, p->split[k]));
+      PIC_TRY(make_split(ctx, g, dsp[k], p->max_groups, p->min_group_bytes, s, p->split[k]));
 
   // array ranges: 0 = J (output only), 1 = EB, then the species group by group
   std::vector<Slot>    slots;
@@ -463,7 +480,8 @@ int pic_srpic_step_host(pic_ctx* ctx, pic_host_pipe* p, pic_species* hsp, pic_sp
       // anew and copy out by the new ranges, which the next call reads by.
       // Every input copy of this call has ended (the sort synchronised the
       // stream after the pushes that waited for them).
-      for (int k = 0; k < nspecies; ++k) PIC_TRY(make_split(ctx, dsp[k], s, p->split[k]));
+      for (int k = 0; k < nspecies; ++k)
+        PIC_TRY(make_split(ctx, g, dsp[k], p->max_groups, p->min_group_bytes, s, p->split[k]));
       build();
       if (p->out_done.size() != slots.size() || p->ch_in.size() != first.size() - 1)
         PIC_TRY(reset_events(p, slots.size(), first.size() - 1));

@@ -96,6 +96,10 @@ class HostPipe:
     def sync(self):
         abi.call("pic_host_pipe_sync", self.h)
 
+    def set_groups(self, max_groups, min_group_bytes):
+        """pic_host_pipe_set_groups: how binned species are cut into groups."""
+        abi.call("pic_host_pipe_set_groups", self.h, int(max_groups), int(min_group_bytes))
+
     def bytes(self):
         """(host-to-device, device-to-host) bytes of the last step."""
         a, b = C.c_int64(0), C.c_int64(0)

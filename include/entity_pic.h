@@ -340,6 +340,11 @@ int pic_host_pipe_destroy(pic_host_pipe* pipe);
 /* Waits for every copy the pipe has queued; the host arrays then hold the
  * last step's result. */
 int pic_host_pipe_sync(pic_host_pipe* pipe);
+/* How binned species are cut into tile groups: at most max_groups groups
+ * (default 8) of at least min_group_bytes of particle state each (default
+ * 256 MiB). Fewer, larger groups suit small species; more groups overlap the
+ * copies and the push more finely. */
+int pic_host_pipe_set_groups(pic_host_pipe* pipe, int32_t max_groups, int64_t min_group_bytes);
 /* Bytes the last pic_srpic_step_host call copied host to device and back. */
 int pic_host_pipe_bytes(const pic_host_pipe* pipe, int64_t* bytes_in, int64_t* bytes_out);
 

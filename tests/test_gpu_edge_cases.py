@@ -148,3 +148,42 @@ def test_sort_without_waiting_matches_the_waiting_sort():
     assert cb.sort(b, fl | abi.PIC_SORT_NO_SYNC) == abi.PIC_OK
     torch.cuda.synchronize()
     assert cb.device_errors(reset=True)[1] == 1
+
+
+def test_tile_range_entry_points():
+    """pic_tile_offsets / pic_push_deposit_tiles: refused without a tiled
+    binning or with a bad range; covering the tiles in pieces gives the same
+    particles as one pic_push_deposit."""
+    g = GridSpec(dim=2, n=(48, 32, 1), order=1, real=torch.float64)
+    L = abi.load()
+    ctx = Context(g)
+    sp = make_species(g, 4, 0.2, 0.2, 23, device="cuda", with_prev=False)
+    nt = C.c_int64(0)
+    ps = mk(sp, 2)
+    assert L.pic_tile_offsets(ctx.h, C.byref(ps), None, 0, C.byref(nt), None) == \
+        abi.PIC_ERR_UNSUPPORTED
+    EB = random_fields(g, 8, amp=0.05).cuda()
+    J = empty_field(g, 3, "cuda")
+    args = (C.c_void_p(EB.data_ptr()), C.c_void_p(J.data_ptr()), 0.3, 1.0, 1.0)
+    assert L.pic_push_deposit_tiles(ctx.h, C.byref(ps), *args, 0, 1, 0, None) == \
+        abi.PIC_ERR_UNSUPPORTED
+    assert ctx.sort(sp, abi.PIC_SORT_SPATIAL | abi.PIC_SORT_TILED | abi.PIC_SORT_SKIP_PREV) == \
+        abi.PIC_OK
+    ps = mk(sp, 2)
+    assert L.pic_tile_offsets(ctx.h, C.byref(ps), None, 0, C.byref(nt), None) == abi.PIC_OK
+    n = nt.value
+    off = (C.c_int32 * (n + 1))()
+    assert L.pic_tile_offsets(ctx.h, C.byref(ps), off, n + 1, C.byref(nt), None) == abi.PIC_OK
+    assert off[0] == 0 and off[n] == sp.npart and all(off[t] <= off[t + 1] for t in range(n))
+    assert L.pic_push_deposit_tiles(ctx.h, C.byref(ps), *args, 0, n + 1, 0, None) == \
+        abi.PIC_ERR_ARG
+    ref = sp.clone()
+    Jr = empty_field(g, 3, "cuda")
+    ctx.push_deposit([ref], EB, Jr, 0.3, 1.0, 1.0)
+    for lo, hi in ((0, n // 3), (n // 3, n // 2), (n // 2, n)):
+        st = L.pic_push_deposit_tiles(ctx.h, C.byref(ps), *args, lo, hi,
+                                      abi.PIC_PD_NO_ZERO if lo else 0, None)
+        assert st == abi.PIC_OK
+    torch.cuda.synchronize()
+    _assert_particles_equal(ref.to("cpu"), sp, 2, prev=False)
+    assert float((J - Jr).abs().max()) <= 1e-12 * float(Jr.abs().max())

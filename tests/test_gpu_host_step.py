@@ -64,6 +64,7 @@ def test_host_resident_steps_match_device_steps(dim, sort_tiled, clear, deposit)
     EBb = torch.full_like(EBa, 7.0)
     Jb, Bb = empty_field(g, 3, "cuda"), empty_field(g, 3, "cuda")
     pipe = HostPipe()
+    pipe.set_groups(4, 1)   # small species: still several groups each
     for k in range(nsteps):
         ctx2.step_host(pipe, hs, ds, hEB, EBb, hJ, Jb, Bb, prm, k)
     pipe.sync()
