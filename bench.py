@@ -70,6 +70,13 @@ WORKLOADS = {
                    cfl=0.5, skindepth0=0.05, larmor0=0.0025, ppc0=2.0, niter=10,
                    sort_interval=0, clear_interval=100, precision_n=(512, 256),
                    precision_steps=200),
+    # particle injection and output preparation on the turbulence state (one
+    # species pair of 8 ppc each on 256^3): not a step, each kernel timed alone
+    "io3d": dict(name="3D injection and output preparation on the 256^3 turbulence state, "
+                      "e-/e+ 8 ppc each, FP32", dim=3, n=(256, 256, 256), order=2, ppc=8,
+                 temp=0.09, drift=0.0, nfilter=4, cfl=0.45, skindepth0=10.0, larmor0=10.0,
+                 ppc0=16.0, field="turbulent", modes=8, dB=1.0, bench_steps=5,
+                 sort_interval=8),
     "sweep3d": dict(name="3D SR magnetized uniform plasma 192^3, e-/e+ 32 ppc each, sigma 10, "
                          "theta 1, order 3, FP32 vs FP64", dim=3, n=(192, 192, 192), order=3,
                     ppc=32, temp=1.0, drift=0.0, nfilter=0, cfl=0.45, skindepth0=10.0,
@@ -715,6 +722,124 @@ def run_sweep(args, w):
     print(json.dumps(line), flush=True)
 
 
+def run_io(args, w):
+    """Injection and output preparation, each timed alone with CUDA events
+    on a resident state larger than L2; algorithmic bytes per call against
+    the measured HBM peak."""
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from __graft_entry__ import build
+    build()
+    from entity_gb300 import abi
+    from entity_gb300.inputs import empty_field, empty_species, inject_params
+    from entity_gb300.sim import Context
+    lib = abi.load()
+    g, EB, J, buff, sp = make_setup(w, "cuda", n=args.cells)
+    prm = step_prm(g, w, w["sort_interval"], sort_tiled=True)
+    ctx = Context(g)
+    ctx.step(sp, EB, J, buff, prm, 0)   # fills the ghosts and tile-sorts
+    torch.cuda.synchronize()
+    npart = sum(s.npart for s in sp)
+    ncells = g.ncells()
+    rb = 4
+    peak, peak_src = hbm_peak()
+    reps = max(3, args.steps)
+    launches0 = lib.pic_kernel_launches()
+    sampler = ClockSampler(local)
+    sampler.start()
+
+    def timed(fn, nbytes, per):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        gbs = nbytes / (ms / 1e3) / 1e9
+        return {"ms": ms, "GB/s": gbs, "frac": gbs / peak, "bytes_per_call": nbytes,
+                "algorithmic_bytes": per}
+
+    out = {}
+    # injection: both species of a pair appended to empty species, i, dx, u,
+    # w, tag written per particle (the prev arrays are not written)
+    cap = sp[0].npart
+    e1 = empty_species(g, cap, charge=-1.0, index=1)
+    e2 = empty_species(g, cap, charge=1.0, index=2)
+    ip = inject_params(1.0, 2.0 * w["ppc"], [(0, g.n[d]) for d in range(3)],
+                       (w["temp"], w["temp"]), seed=9)
+    per_inj = 3 * 4 + 3 * 4 + 4 * rb + 2
+
+    def inject():
+        e1.npart = e2.npart = 0
+        ctx.inject_uniform_maxwellians(e1, e2, ip)
+    inject()
+    torch.cuda.synchronize()
+    out["pic_inject_uniform_maxwellians"] = timed(inject, (e1.npart + e2.npart) * per_inj,
+                                                  f"{per_inj} B written per particle")
+    out["pic_inject_uniform_maxwellians"]["particles_per_s"] = (
+        (e1.npart + e2.npart) / (out["pic_inject_uniform_maxwellians"]["ms"] / 1e3))
+    del e1, e2
+    torch.cuda.empty_cache()
+    # moments: N at order 2 (27 cells per particle), T^{0i} at order 0
+    bckp = empty_field(g, 6, "cuda")
+
+    def mom(mid, order, c1=0, c2=0):
+        p = abi.PicMomentParams()
+        p.id, p.c1, p.c2, p.order, p.smoothing = mid, c1, c2, order, abi.PIC_SMOOTH_SPLINE
+        p.use_weights, p.inv_n0, p.dx = 1, 1.0 / w["ppc0"], g.dx
+        return p
+    pn, pt = mom(abi.PIC_MOM_N, 2), mom(abi.PIC_MOM_T, 0, 0, 1)
+    per_n = 3 * 4 + 3 * 4 + rb + 2
+    out["pic_output_moment N order 2"] = timed(
+        lambda: ctx.output_moment(sp, pn, bckp, 0), npart * per_n + ncells * 4,
+        f"{per_n} B read per particle + 4 B per cell")
+    per_t = per_n + 3 * rb
+    out["pic_output_moment T01 order 0"] = timed(
+        lambda: ctx.output_moment(sp, pt, bckp, 1), npart * per_t + ncells * 4,
+        f"{per_t} B read per particle + 4 B per cell")
+    out["pic_sync_moments"] = timed(lambda: ctx.sync_moments(bckp, 0, 2), 0, "ghost slabs only")
+    # fields at cell centres in the tetrad basis, no downsampling
+    fo = torch.empty((3,) + tuple(reversed(g.n)), dtype=g.real, device="cuda")
+    flags = abi.PIC_OUT_INTERP_EDGES | abi.PIC_OUT_TO_HAT
+    out["pic_output_field E"] = timed(
+        lambda: ctx.output_field(EB, 1, 0, 3, flags, g.dx, (1, 1, 1), fo), ncells * 24,
+        "12 B read + 12 B written per cell")
+    # every particle as a record in physical units (stride 1)
+    n0 = sp[0].npart
+    xs = [torch.empty(n0, dtype=g.real, device="cuda") for _ in range(3)]
+    us = [torch.empty(n0, dtype=g.real, device="cuda") for _ in range(3)]
+    ws = torch.empty(n0, dtype=g.real, device="cuda")
+    per_p = (3 * 4 + 3 * 4 + 4 * rb) + 7 * rb
+    out["pic_output_particles stride 1"] = timed(
+        lambda: ctx.output_particles(sp[0], 1, g.dx, (0.0, 0.0, 0.0), xs, us, ws), n0 * per_p,
+        f"{per_p} B per particle (i, dx, u, w read; x, u, w written)")
+    clocks = sampler.stop()
+    launches = lib.pic_kernel_launches() - launches0
+    top = out["pic_output_moment N order 2"]
+    line = {
+        "metric": "output-preparation throughput (particle moments, fields, particle "
+                  "records) and device injection on 1 GB300",
+        "value": npart / (top["ms"] / 1e3), "unit": "particles/s (N moment, order 2)",
+        "n_gpus": 1, "steps": reps, "warmup": args.warmup, "ms_per_step": top["ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": w["name"], "cells": ncells,
+                                        "particles_per_gpu": npart,
+                                        "l2": "inputs larger than L2"},
+        "kernels": out,
+        "roofline": {"bound": "hbm", "achieved": top["GB/s"], "peak": peak, "unit": "GB/s",
+                     "frac": top["frac"], "traffic": None,
+                     "kernel": "k_output_moment (N, order 2, global atomics)",
+                     "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_src})"},
+        "cpu_baseline": None, "e2e": None, "gpu_launches": launches, "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -758,6 +883,8 @@ def main():
         run_adjoint(args, w)
     elif args.workload == "wald2d":
         run_wald(args, w)
+    elif args.workload == "io3d":
+        run_io(args, w)
     else:
         run_ours(args, w)
 
