@@ -187,7 +187,11 @@ cudaError_t copy_field(void* dst, const void* src, size_t bytes, cudaMemcpyKind 
   if (!hd || bytes == 0) return bytes ? cudaMemcpyAsync(dst, src, bytes, kind, q) : cudaSuccess;
   const unsigned char* s = (const unsigned char*)(kind == cudaMemcpyHostToDevice ? hd : src);
   unsigned char*       d = (unsigned char*)(kind == cudaMemcpyHostToDevice ? dst : hd);
-  k_copy_bytes<<<152 * 4, 256, 0, q>>>(s, d, bytes);
+  int dev = 0, sms = 0;  // four blocks per SM stream the link at full rate
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+    return cudaMemcpyAsync(dst, src, bytes, kind, q);
+  k_copy_bytes<<<sms * 4, 256, 0, q>>>(s, d, bytes);
   pic::note_launch();
   return cudaGetLastError();
 }
