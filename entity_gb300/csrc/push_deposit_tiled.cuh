@@ -110,7 +110,10 @@ struct FixedAcc<double> {
 // must fit one CTA's 227 KB
 template <int D, typename real, int O>
 struct TileShape {
-  static constexpr int X = 32, Y = 32, Z = 1, NT = 256;  // 2D
+  // 2D: 16 x 8 cells. The 512^2 pair plasma (2 x 16 ppc) ran push+deposit in
+  // 0.578 ms with 32 x 32 tiles (256 CTAs, 0.56 waves), 0.456 ms with
+  // 16 x 16, 0.419 ms with 16 x 8 and 0.429 ms with 8 x 8
+  static constexpr int X = 16, Y = 8, Z = 1, NT = 256;
 };
 // 3D FP32 at order 3: 8^3 cells, so that two copies of the J window fit
 // (measured on the 96^3 sweep plasma, 2 x 32 ppc: 28.1 ms per step against
