@@ -275,10 +275,10 @@ __global__ void __launch_bounds__(256) k_push_deposit_adjoint(AdjArgs<real> a) {
 #pragma unroll
           for (int ai = 0; ai < O + 1; ai++) {
             const real F = a.EB.ld(m0 + ai, m1 + bj, 0, c);
-            r            = rfma(s0 ? Sd[0][ai] : Sp[0][ai], F, r);
+            r            = iacc(s0 ? Sd[0][ai] : Sp[0][ai], F, r);
             rd += (s0 ? dSd[0][ai] : dSp[0][ai]) * F;
           }
-          v = rfma(r, s1 ? Sd[1][bj] : Sp[1][bj], v);
+          v = iacc(r, s1 ? Sd[1][bj] : Sp[1][bj], v);
           d0 += (s1 ? Sd[1][bj] : Sp[1][bj]) * rd;
           d1 += (s1 ? dSd[1][bj] : dSp[1][bj]) * r;
         }

@@ -67,8 +67,8 @@ __device__ __forceinline__ void interp_db(const FieldView<real>& em, const Field
     for (int b = 0; b < O + 1; b++) {
       real c0 = 0;
 #pragma unroll
-      for (int a = 0; a < O + 1; a++) c0 = rfma(s0 ? Sd[0][a] : Sp[0][a], F.ld(m0 + a, m1 + b, 0, c), c0);
-      v = rfma(c0, s1 ? Sd[1][b] : Sp[1][b], v);
+      for (int a = 0; a < O + 1; a++) c0 = iacc(s0 ? Sd[0][a] : Sp[0][a], F.ld(m0 + a, m1 + b, 0, c), c0);
+      v = iacc(c0, s1 ? Sd[1][b] : Sp[1][b], v);
     }
     if (c < 3) Dv[c] = v;
     else Bv[c - 3] = v;

@@ -29,8 +29,13 @@ struct K<double> {
   static constexpr double THIRD = 0.3333333333333333;
 };
 
-__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-__device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+// one term of an interpolation sum, `c += a * b` as the reference writes it
+// (src/kernels/pushers/sr.hpp:1118-1369, gr.hpp:594-662): the product and the
+// sum round separately (the library is built with -fmad=false)
+template <typename real>
+__device__ __forceinline__ real iacc(real a, real b, real c) {
+  return c + a * b;
+}
 
 // staggering of (ex1, ex2, ex3, bx1, bx2, bx3) per axis: 1 = dual
 // (src/kernels/pushers/sr.hpp:1210-1366)
@@ -212,6 +217,12 @@ __device__ __forceinline__ void interp_zigzag(const V& EB, const int* ic,
         wp[a] = wpp[a];
       }
     }
+    if (D == 3 && c == 5) {
+      // the reference's 3D Bx3 (sr.hpp:1100-1116) reads the dual x2 stencil
+      // (j - 1 + indy, j + indy) with the primal weights ponpmy / ponppy
+      wm[1] = wpm[1];
+      wp[1] = wpp[1];
+    }
     real v;
     if constexpr (D == 2) {
       // sr.hpp:905-977
@@ -247,7 +258,7 @@ __device__ __forceinline__ void interp_zigzag(const V& EB, const int* ic,
 template <int D, int O, typename real, typename V>
 __device__ __forceinline__ void interp_shape(const V& EB, const int* ic,
                                              const real* dc, real* e0, real* b0) {
-  // sr.hpp:1151-1369; running sums as fma(S, EB, c)
+  // sr.hpp:1151-1369; running sums c += S * EB, rounded separately
   int  pmin[3] = { 0, 0, 0 }, dmin[3] = { 0, 0, 0 };
   real Sp[3][O + 1], Sd[3][O + 1];
 #pragma unroll
@@ -267,9 +278,9 @@ __device__ __forceinline__ void interp_shape(const V& EB, const int* ic,
         real c0 = 0;
 #pragma unroll
         for (int a = 0; a < O + 1; a++) {
-          c0 = rfma(s0 ? Sd[0][a] : Sp[0][a], EB.ld(m0 + a, m1 + b, 0, c), c0);
+          c0 = iacc(s0 ? Sd[0][a] : Sp[0][a], EB.ld(m0 + a, m1 + b, 0, c), c0);
         }
-        v = rfma(c0, s1 ? Sd[1][b] : Sp[1][b], v);
+        v = iacc(c0, s1 ? Sd[1][b] : Sp[1][b], v);
       }
     } else {
       const int m2 = s2 ? dmin[2] : pmin[2];
@@ -281,11 +292,11 @@ __device__ __forceinline__ void interp_shape(const V& EB, const int* ic,
           real c00 = 0;
 #pragma unroll
           for (int a = 0; a < O + 1; a++) {
-            c00 = rfma(s0 ? Sd[0][a] : Sp[0][a], EB.ld(m0 + a, m1 + b, m2 + cc, c), c00);
+            c00 = iacc(s0 ? Sd[0][a] : Sp[0][a], EB.ld(m0 + a, m1 + b, m2 + cc, c), c00);
           }
-          c0 = rfma(c00, s1 ? Sd[1][b] : Sp[1][b], c0);
+          c0 = iacc(c00, s1 ? Sd[1][b] : Sp[1][b], c0);
         }
-        v = rfma(c0, s2 ? Sd[2][cc] : Sp[2][cc], v);
+        v = iacc(c0, s2 ? Sd[2][cc] : Sp[2][cc], v);
       }
     }
     if (c < 3) e0[c] = v; else b0[c - 3] = v;
@@ -437,13 +448,11 @@ __device__ __forceinline__ bool deposit_with_velocity(const Prtl<real>& q, const
                                                       real weight, real charge, real inv_dt,
                                                       int ng, const int* ext, Add&& add);
 
-template <int D, int O, typename real, typename Add>
-__device__ __forceinline__ bool deposit_particle(const Prtl<real>& q, real weight, real charge,
-                                                 real inv_dt, real dx, int ng, const int* ext,
-                                                 Add&& add) {
+// Cartesian velocity of the deposit (currents_deposit.hpp:130-165); only the
+// unsimulated direction's component enters a 2D deposit
+template <int D, typename real>
+__device__ __forceinline__ void deposit_velocity(const Prtl<real>& q, real dx, real* vp) {
   const real ONE = 1, ZERO = 0;
-  // Cartesian velocity for the unsimulated direction (currents_deposit.hpp:130-165)
-  real       vp[3];
   vp[0] = q.u[0] / dx;
   vp[1] = q.u[1] / dx;
   vp[2] = (D == 3) ? q.u[2] / dx : q.u[2];
@@ -452,7 +461,125 @@ __device__ __forceinline__ bool deposit_particle(const Prtl<real>& q, real weigh
   vp[0] *= inv_energy;
   vp[1] *= inv_energy;
   vp[2] *= inv_energy;
+}
+
+template <int D, int O, typename real, typename Add>
+__device__ __forceinline__ bool deposit_particle(const Prtl<real>& q, real weight, real charge,
+                                                 real inv_dt, real dx, int ng, const int* ext,
+                                                 Add&& add) {
+  real vp[3];
+  deposit_velocity<D, real>(q, dx, vp);
   return deposit_with_velocity<D, O, real>(q, vp, weight, charge, inv_dt, ng, ext, add);
+}
+
+// Esirkepov deposit (orders 1-3) of a particle whose initial and final
+// stencils start at the same cell along every axis: for_deposit's third case
+// (particle_shapes.hpp:1001-1015), where the (O+2)-th row of both stencils is
+// empty and the extents are O. Only the (O+1)^D box is visited, so no entry
+// carries a predicate. iS/fS are the O+1 weights of the two stencils along
+// each axis, i0 the ghost-inclusive index of their first cell. Every entry's
+// value is the expression deposit_with_velocity forms for it, so J is the same
+// as the general loop's.
+template <int D, int O, typename real, typename Add>
+__device__ __forceinline__ void deposit_same_support(const real (*iS)[O + 1],
+                                                     const real (*fS)[O + 1], const int* i0,
+                                                     real coeff, real vz, real inv_dt, Add&& add) {
+  constexpr int N    = O + 1;
+  const real    HALF = 0.5, THIRD = K<real>::THIRD;
+  const real    Q    = coeff * inv_dt;
+  if constexpr (D == 2) {
+    const real QVx3 = coeff * vz;
+    real       hd0[N], hs0[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      hd0[i] = HALF * (fS[0][i] - iS[0][i]);
+      hs0[i] = HALF * (fS[0][i] + iS[0][i]);
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      const real s1  = fS[1][j] + iS[1][j];
+      real       acc = 0;
+#pragma unroll
+      for (int i = 0; i < N - 1; ++i) {
+        const real W = hd0[i] * s1;
+        acc          = (i == 0) ? (-Q * W) : (acc - Q * W);
+        add(i0[0] + i, i0[1] + j, 0, 0, acc);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      real acc = 0;
+#pragma unroll
+      for (int j = 0; j < N - 1; ++j) {
+        const real W = hs0[i] * (fS[1][j] - iS[1][j]);
+        acc          = (j == 0) ? (-Q * W) : (acc - Q * W);
+        add(i0[0] + i, i0[1] + j, 0, 1, acc);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const real ga = HALF * iS[0][i] + fS[0][i];
+      const real gb = HALF * fS[0][i] + iS[0][i];
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        const real W = THIRD * (fS[1][j] * ga + iS[1][j] * gb);
+        add(i0[0] + i, i0[1] + j, 0, 2, QVx3 * W);
+      }
+    }
+  } else {
+    real t0[N], t1[N], t2[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      t0[i] = THIRD * (fS[0][i] - iS[0][i]);
+      t1[i] = THIRD * (fS[1][i] - iS[1][i]);
+      t2[i] = THIRD * (fS[2][i] - iS[2][i]);
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        const real P = (iS[1][j] * iS[2][k] + fS[1][j] * fS[2][k]) +
+                       HALF * (iS[2][k] * fS[1][j] + iS[1][j] * fS[2][k]);
+        real acc = 0;
+#pragma unroll
+        for (int i = 0; i < N - 1; ++i) {
+          const real W = t0[i] * P;
+          acc          = (i == 0) ? (-Q * W) : (acc - Q * W);
+          add(i0[0] + i, i0[1] + j, i0[2] + k, 0, acc);
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        const real P = iS[0][i] * iS[2][k] + fS[0][i] * fS[2][k] +
+                       HALF * (iS[2][k] * fS[0][i] + iS[0][i] * fS[2][k]);
+        real acc = 0;
+#pragma unroll
+        for (int j = 0; j < N - 1; ++j) {
+          const real W = t1[j] * P;
+          acc          = (j == 0) ? (-Q * W) : (acc - Q * W);
+          add(i0[0] + i, i0[1] + j, i0[2] + k, 1, acc);
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        const real P = iS[0][i] * iS[1][j] + fS[0][i] * fS[1][j] +
+                       HALF * (iS[0][i] * fS[1][j] + iS[1][j] * fS[0][i]);
+        real acc = 0;
+#pragma unroll
+        for (int k = 0; k < N - 1; ++k) {
+          const real W = t2[k] * P;
+          acc          = (k == 0) ? (-Q * W) : (acc - Q * W);
+          add(i0[0] + i, i0[1] + j, i0[2] + k, 2, acc);
+        }
+      }
+    }
+  }
 }
 
 // the deposit proper, given the particle velocity vp (the GR deposit passes

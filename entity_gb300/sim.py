@@ -10,6 +10,7 @@ allocator here, every computation runs in libentity_pic.so.
 """
 import ctypes as C
 
+import numpy as np
 import torch
 
 from . import abi
@@ -361,11 +362,13 @@ def step_params(g: GridSpec, *, cfl, ppc0, skindepth0, larmor0, nfilter=0, sort_
                 clear_interval=100, correction=1.0, write_prev=False, fieldsolver=True,
                 deposit=True, sort_tiled=False):
     """Scales of SimulationParams (src/framework/parameters/parameters.cpp:47-78,
-    algorithms.cpp:18-27, minkowski.h:82-84) in real_t arithmetic."""
-    R = g.real
-    t = lambda v: torch.tensor(v, dtype=R)
+    algorithms.cpp:18-27, minkowski.h:82-84) in real_t arithmetic: numpy
+    scalars of the real type, whose square root rounds correctly (torch's CPU
+    sqrt of a float64 scalar can be one ulp off)."""
+    R = np.float32 if g.real == torch.float32 else np.float64
+    t = lambda v: R(v)
     dx = t(g.dx)
-    dxmin = dx / torch.sqrt(t(float(g.dim)))
+    dxmin = dx / np.sqrt(t(float(g.dim)))
     dt = t(cfl) * dxmin
     # V0 = sqrt_det_h (minkowski.h:144-152): SQR(dx) in 2D, CUBE(dx) in 3D
     V0 = dx * dx if g.dim == 2 else dx * dx * dx

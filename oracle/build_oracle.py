@@ -1,11 +1,11 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles oracle/srpic_oracle.c, grpic_oracle.c, inject_oracle.c and output_oracle.c twice with gcc into
-oracle/_build/:
-  liboracle_f32.so  (real = float,  the reference's SINGLE_PRECISION build)
-  liboracle_f64.so  (real = double)
-with -ffp-contract=off so every operation is rounded as written, and OpenMP so
-the CPU-baseline leg can use every host core.
+Compiles oracle/srpic_oracle.c, grpic_oracle.c, inject_oracle.c and
+output_oracle.c with gcc into oracle/_build/:
+  liboracle_f32.so      (real = float, the reference's SINGLE_PRECISION build)
+  liboracle_f64.so      (real = double)
+all with -ffp-contract=off so every operation is rounded as written, and
+OpenMP so the CPU-baseline leg can use every host core.
 """
 import os
 import subprocess

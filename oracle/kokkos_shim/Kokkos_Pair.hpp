@@ -1,0 +1,3 @@
+// Kokkos API shim (test infrastructure): Kokkos_Pair.hpp is covered by Kokkos_Core.hpp.
+#pragma once
+#include "Kokkos_Core.hpp"

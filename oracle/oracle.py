@@ -8,6 +8,7 @@ import ctypes as C
 import math
 import os
 
+import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -307,7 +308,9 @@ class Oracle:
         if step == 0:
             self.fill_ghosts(EB, True, 0, 6)
         dT = t(0.5) * t(prm.correction) * t(prm.dt)
-        dxm = torch.sqrt(t(prm.dx) * t(prm.dx))
+        # dx = sqrt(h_11) (fieldsolvers.h:50), rounded correctly
+        npR = np.float32 if R == torch.float32 else np.float64
+        dxm = t(float(np.sqrt(npR(prm.dx) * npR(prm.dx))))
         c1 = dT / (dxm * dxm) if g.dim == 2 else dT / dxm
         c2 = dT if g.dim == 2 else t(0.0)
         if prm.fieldsolver_enabled:

@@ -1,0 +1,357 @@
+// Entity's own SR kernels, compiled unmodified from the reference sources
+// against the host Kokkos shim in oracle/kokkos_shim (TEST INFRASTRUCTURE).
+//
+// This translation unit contains no physics of its own: each entry point
+// wraps the caller's arrays in shim Views and runs the reference's functor the
+// way the reference's host wrapper launches it. The entry points take the
+// oracle's grid and species structs (srpic_oracle.h), so the tests can run the
+// restated oracle and the reference's code on identical inputs.
+//
+// Built by oracle/build_ref.py once per (precision, SHAPE_ORDER), because the
+// reference fixes both at compile time (cmake/config.cmake:4-28): the shape
+// order selects the pusher's interpolation and N_GHOSTS (global.h:130-136).
+#include "enums.h"
+#include "global.h"
+
+#include "arch/kokkos_aliases.h"
+#include "metrics/minkowski.h"
+#include "utils/sorting.h"
+
+#include "kernels/ampere_mink.hpp"
+#include "kernels/currents_deposit.hpp"
+#include "kernels/digital_filter.hpp"
+#include "kernels/faraday_mink.hpp"
+#include "kernels/pushers/sr.hpp"
+
+#include "srpic_oracle.h"
+
+#include <cstdint>
+#include <vector>
+
+namespace {
+  using namespace ntt;
+
+  template <typename T>
+  array_t<T*> wrap1(void* p, std::int64_t n) {
+    if (p == nullptr) {
+      return array_t<T*> {};
+    }
+    return array_t<T*>(static_cast<T*>(p), static_cast<std::size_t>(n));
+  }
+
+  // ghost-inclusive field of N components with the oracle's strides
+  template <Dimension D, unsigned short N>
+  ndfield_t<D, N> wrap_field(const orc_grid* g, const void* p, const int64_t* s) {
+    const std::size_t ng = (std::size_t)g->ng;
+    std::size_t       ext[4], st[4];
+    ext[0] = (std::size_t)g->n1 + 2 * ng;
+    st[0]  = (std::size_t)s[0];
+    ext[1] = (std::size_t)g->n2 + 2 * ng;
+    st[1]  = (std::size_t)s[1];
+    if constexpr (D == Dim::_3D) {
+      ext[2] = (std::size_t)g->n3 + 2 * ng;
+      st[2]  = (std::size_t)s[2];
+    }
+    ext[D] = N;
+    st[D]  = (std::size_t)s[3];
+    return ndfield_t<D, N>::wrap_strided(static_cast<real_t*>(const_cast<void*>(p)), ext, st);
+  }
+
+  template <Dimension D>
+  metric::Minkowski<D> make_metric(const orc_grid* g, double dx) {
+    std::vector<ncells_t> res { (ncells_t)g->n1, (ncells_t)g->n2 };
+    boundaries_t<real_t>  ext { { ZERO, (real_t)g->n1 * (real_t)dx },
+                                { ZERO, (real_t)g->n2 * (real_t)dx } };
+    if constexpr (D == Dim::_3D) {
+      res.push_back((ncells_t)g->n3);
+      ext.push_back({ ZERO, (real_t)g->n3 * (real_t)dx });
+    }
+    return metric::Minkowski<D>(res, ext);
+  }
+
+  template <Dimension D>
+  range_t<D> active_range(const orc_grid* g) {
+    if constexpr (D == Dim::_2D) {
+      return range_t<D>({ N_GHOSTS, N_GHOSTS },
+                        { N_GHOSTS + (ncells_t)g->n1, N_GHOSTS + (ncells_t)g->n2 });
+    } else {
+      return range_t<D>({ N_GHOSTS, N_GHOSTS, N_GHOSTS },
+                        { N_GHOSTS + (ncells_t)g->n1,
+                          N_GHOSTS + (ncells_t)g->n2,
+                          N_GHOSTS + (ncells_t)g->n3 });
+    }
+  }
+
+  PrtlBC prtl_bc(int code) {
+    switch (code) {
+      case 0:
+        return PrtlBC::PERIODIC;
+      case 1:
+        return PrtlBC::ABSORB;
+      case 2:
+        return PrtlBC::REFLECT;
+      default:
+        return PrtlBC::AXIS;
+    }
+  }
+
+  FldsBC flds_bc(int code) {
+    switch (code) {
+      case 0:
+        return FldsBC::PERIODIC;
+      case 2:
+        return FldsBC::CONDUCTOR;
+      case 3:
+        return FldsBC::MATCH;
+      default:
+        return FldsBC::FIXED;
+    }
+  }
+
+  ParticleArrays arrays_of(const orc_species* sp) {
+    ParticleArrays a;
+    const auto     n = sp->npart;
+    a.i1             = wrap1<int>(sp->i1, n);
+    a.i2             = wrap1<int>(sp->i2, n);
+    a.i3             = wrap1<int>(sp->i3, n);
+    a.i1_prev        = wrap1<int>(sp->i1_prev, n);
+    a.i2_prev        = wrap1<int>(sp->i2_prev, n);
+    a.i3_prev        = wrap1<int>(sp->i3_prev, n);
+    a.dx1            = wrap1<prtldx_t>(sp->dx1, n);
+    a.dx2            = wrap1<prtldx_t>(sp->dx2, n);
+    a.dx3            = wrap1<prtldx_t>(sp->dx3, n);
+    a.dx1_prev       = wrap1<prtldx_t>(sp->dx1_prev, n);
+    a.dx2_prev       = wrap1<prtldx_t>(sp->dx2_prev, n);
+    a.dx3_prev       = wrap1<prtldx_t>(sp->dx3_prev, n);
+    a.ux1            = wrap1<real_t>(sp->ux1, n);
+    a.ux2            = wrap1<real_t>(sp->ux2, n);
+    a.ux3            = wrap1<real_t>(sp->ux3, n);
+    a.weight         = wrap1<real_t>(sp->weight, n);
+    a.tag            = wrap1<short>(sp->tag, n);
+    return a;
+  }
+
+  // srpic::ParticlePush (src/engines/srpic/particle_pusher.h:35-185) for one
+  // species without atmosphere, drag or emission: PusherContext, the particle
+  // boundaries of the mesh, the default policy, one parallel_for
+  template <Dimension D>
+  void push(const orc_grid* g, orc_species* sp, const void* EB, double dt, double omegaB0,
+            double dx) {
+    using M = metric::Minkowski<D>;
+    ParticlePusherFlags flags = ParticlePusher::NONE;
+    if (sp->pusher == ORC_PUSHER_BORIS) {
+      flags = ParticlePusher::BORIS;
+    } else if (sp->pusher == ORC_PUSHER_VAY) {
+      flags = ParticlePusher::VAY;
+    } else if (sp->pusher == ORC_PUSHER_PHOTON) {
+      flags = ParticlePusher::PHOTON;
+    }
+    if (flags == ParticlePusher::NONE || sp->npart == 0) {
+      return;
+    }
+    kernel::sr::PusherContext ctx { 1u,
+                                    flags,
+                                    RadiativeDrag::NONE,
+                                    sp->mass,
+                                    sp->charge,
+                                    0.0,
+                                    (real_t)dt,
+                                    (real_t)omegaB0,
+                                    g->n1,
+                                    g->n2,
+                                    D == Dim::_3D ? g->n3 : 1 };
+    boundaries_t<PrtlBC> bcs;
+    for (int d = 0; d < (int)D; ++d) {
+      bcs.push_back({ prtl_bc(g->prtl_bc[d][0]), prtl_bc(g->prtl_bc[d][1]) });
+    }
+    kernel::sr::PusherBoundaries<D> bnd { bcs };
+    ParticleArrays                  arrays = arrays_of(sp);
+    const auto                      em     = wrap_field<D, 6>(g, EB, g->em_s);
+    const M                         metric = make_metric<D>(g, dx);
+    using P                                = kernel::sr::PusherPolicy<M>;
+    Kokkos::parallel_for("ParticlePusher",
+                         Kokkos::RangePolicy<Kokkos::DefaultExecutionSpace>(0, sp->npart),
+                         kernel::sr::Pusher_kernel<M, P> { ctx, bnd, arrays, em, metric, P {} });
+  }
+
+  // srpic::CurrentsDeposit (src/engines/srpic/currents.h:32-87) for one
+  // species into J (not zeroed here): a scatter view, the deposit kernel at
+  // the build's shape order, contribute
+  template <Dimension D>
+  void deposit(const orc_grid* g, const orc_species* sp, void* J, double dt, double dx) {
+    using M = metric::Minkowski<D>;
+    if (sp->npart == 0 || sp->pusher == ORC_PUSHER_NONE || sp->charge == 0.0f) {
+      return;
+    }
+    auto       cur         = wrap_field<D, 3>(g, J, g->cur_s);
+    auto       scatter_cur = Kokkos::Experimental::create_scatter_view(cur);
+    const auto a           = arrays_of(sp);
+    const M    metric      = make_metric<D>(g, dx);
+    Kokkos::parallel_for(
+      "CurrentsDeposit",
+      Kokkos::RangePolicy<Kokkos::DefaultExecutionSpace>(0, sp->npart),
+      kernel::DepositCurrents_kernel<SimEngine::SRPIC, M, SHAPE_ORDER>(
+        scatter_cur, a.i1, a.i2, a.i3, a.i1_prev, a.i2_prev, a.i3_prev, a.dx1, a.dx2, a.dx3,
+        a.dx1_prev, a.dx2_prev, a.dx3_prev, a.ux1, a.ux2, a.ux3, array_t<real_t*> {}, a.weight,
+        a.tag, metric, (real_t)sp->charge, (real_t)dt));
+    Kokkos::Experimental::contribute(cur, scatter_cur);
+  }
+
+  template <Dimension D>
+  void faraday(const orc_grid* g, void* EB, double coeff1, double coeff2, const double* st) {
+    auto em = wrap_field<D, 6>(g, EB, g->em_s);
+    real_t s[9] = { ZERO, ZERO, ZERO, ZERO, ZERO, ZERO, ZERO, ZERO, ZERO };
+    if (st != nullptr) {
+      for (int k = 0; k < 9; ++k) {
+        s[k] = (real_t)st[k];
+      }
+    }
+    Kokkos::parallel_for("Faraday",
+                         active_range<D>(g),
+                         kernel::mink::Faraday_kernel<D>(em,
+                                                         (real_t)coeff1,
+                                                         (real_t)coeff2,
+                                                         s[0], s[1], s[2], s[3], s[4],
+                                                         s[5], s[6], s[7], s[8]));
+  }
+
+  template <Dimension D>
+  void ampere(const orc_grid* g, void* EB, double coeff1, double coeff2) {
+    auto em = wrap_field<D, 6>(g, EB, g->em_s);
+    Kokkos::parallel_for("Ampere",
+                         active_range<D>(g),
+                         kernel::mink::Ampere_kernel<D>(em, (real_t)coeff1, (real_t)coeff2));
+  }
+
+  template <Dimension D>
+  void currents_ampere(const orc_grid* g, void* EB, void* J, double coeff, double ppc0) {
+    auto em  = wrap_field<D, 6>(g, EB, g->em_s);
+    auto cur = wrap_field<D, 3>(g, J, g->cur_s);
+    Kokkos::parallel_for("Ampere",
+                         active_range<D>(g),
+                         kernel::mink::CurrentsAmpere_kernel<D>(em, cur, (real_t)coeff,
+                                                                (real_t)ppc0));
+  }
+
+  // one pass of srpic::CurrentsFilter (src/engines/srpic/currents.h:89-119)
+  // without the ghost exchange that follows it
+  template <Dimension D>
+  void filter_pass(const orc_grid* g, void* J, void* buff) {
+    auto cur = wrap_field<D, 3>(g, J, g->cur_s);
+    auto buf = wrap_field<D, 3>(g, buff, g->cur_s);
+    ncells_t size[D];
+    size[0] = (ncells_t)g->n1;
+    size[1] = (ncells_t)g->n2;
+    if constexpr (D == Dim::_3D) {
+      size[2] = (ncells_t)g->n3;
+    }
+    boundaries_t<FldsBC> bcs;
+    for (int d = 0; d < (int)D; ++d) {
+      bcs.push_back({ flds_bc(g->fbc[d][0]), flds_bc(g->fbc[d][1]) });
+    }
+    Kokkos::deep_copy(buf, cur);
+    Kokkos::parallel_for("CurrentsFilter",
+                         active_range<D>(g),
+                         kernel::DigitalFilter_kernel<D, Coord::Cartesian>(cur, buf, size, bcs));
+  }
+
+  // sort::PositionToTileIndex<D, false> with tile size 1 (the key of
+  // Particles::SortSpatially, src/framework/containers/particles_sort.cpp:196-253)
+  template <Dimension D>
+  void sort_keys(const orc_grid* g, const orc_species* sp, std::uint32_t* keys) {
+    const auto          a = arrays_of(sp);
+    array_t<ncells_t*>  k(reinterpret_cast<ncells_t*>(keys), (std::size_t)sp->npart);
+    std::vector<ncells_t> n { (ncells_t)g->n1, (ncells_t)g->n2 };
+    if constexpr (D == Dim::_3D) {
+      n.push_back((ncells_t)g->n3);
+    }
+    sort::PositionToTileIndex<D, false> f(a.i1, a.i2, a.i3, a.tag, k, n, 1u);
+    Kokkos::parallel_for("Keys",
+                         Kokkos::RangePolicy<Kokkos::DefaultExecutionSpace>(0, sp->npart),
+                         f);
+  }
+
+  template <class F2, class F3>
+  int dispatch(const orc_grid* g, F2&& f2, F3&& f3) {
+    if (g->ng != (int)N_GHOSTS) {
+      return -2;
+    }
+    if (g->dim == 2) {
+      f2();
+    } else if (g->dim == 3) {
+      f3();
+    } else {
+      return -1;
+    }
+    return 0;
+  }
+} // namespace
+
+static_assert(sizeof(ncells_t) == 4, "sort keys are 32-bit");
+
+extern "C" {
+
+int ref_shape_order(void) {
+  return SHAPE_ORDER;
+}
+
+int ref_n_ghosts(void) {
+  return (int)N_GHOSTS;
+}
+
+int ref_real_size(void) {
+  return (int)sizeof(real_t);
+}
+
+int ref_push(const orc_grid* g, orc_species* sp, const void* EB, double dt, double omegaB0,
+             double dx) {
+  return dispatch(
+    g,
+    [&] { push<Dim::_2D>(g, sp, EB, dt, omegaB0, dx); },
+    [&] { push<Dim::_3D>(g, sp, EB, dt, omegaB0, dx); });
+}
+
+int ref_deposit(const orc_grid* g, const orc_species* sp, void* J, double dt, double dx) {
+  return dispatch(
+    g,
+    [&] { deposit<Dim::_2D>(g, sp, J, dt, dx); },
+    [&] { deposit<Dim::_3D>(g, sp, J, dt, dx); });
+}
+
+int ref_faraday(const orc_grid* g, void* EB, double coeff1, double coeff2,
+                const double* stencil) {
+  return dispatch(
+    g,
+    [&] { faraday<Dim::_2D>(g, EB, coeff1, coeff2, stencil); },
+    [&] { faraday<Dim::_3D>(g, EB, coeff1, coeff2, stencil); });
+}
+
+int ref_ampere(const orc_grid* g, void* EB, double coeff1, double coeff2) {
+  return dispatch(
+    g,
+    [&] { ampere<Dim::_2D>(g, EB, coeff1, coeff2); },
+    [&] { ampere<Dim::_3D>(g, EB, coeff1, coeff2); });
+}
+
+int ref_currents_ampere(const orc_grid* g, void* EB, void* J, double coeff, double ppc0) {
+  return dispatch(
+    g,
+    [&] { currents_ampere<Dim::_2D>(g, EB, J, coeff, ppc0); },
+    [&] { currents_ampere<Dim::_3D>(g, EB, J, coeff, ppc0); });
+}
+
+int ref_filter_pass(const orc_grid* g, void* J, void* buff) {
+  return dispatch(
+    g,
+    [&] { filter_pass<Dim::_2D>(g, J, buff); },
+    [&] { filter_pass<Dim::_3D>(g, J, buff); });
+}
+
+int ref_sort_keys(const orc_grid* g, const orc_species* sp, std::uint32_t* keys) {
+  return dispatch(
+    g,
+    [&] { sort_keys<Dim::_2D>(g, sp, keys); },
+    [&] { sort_keys<Dim::_3D>(g, sp, keys); });
+}
+
+} // extern "C"

@@ -14,19 +14,21 @@
 
 #ifdef ORC_SINGLE
 typedef float real;
-#define RFMA  fmaf
 #define RSQRT sqrtf
 #define RFABS fabsf
 /* src/global/utils/numeric.h:31-48 (SINGLE_PRECISION) */
 static const real THIRD = 0.333333f;
 #else
 typedef double real;
-#define RFMA  fma
 #define RSQRT sqrt
 #define RFABS fabs
 /* src/global/utils/numeric.h:50-67 */
 static const real THIRD = 0.3333333333333333;
 #endif
+
+/* one term of the shape-order interpolation sums (sr.hpp:1118-1369,
+ * gr.hpp:594-662): `c += a * b`, product and sum rounded separately */
+#define IACC(a, b, c) ((c) + (a) * (b))
 
 static const real ZERO = 0, ONE = 1, TWO = 2, HALF = 0.5, INV_2 = 0.5;
 static const real INV_4 = 0.25, INV_8 = 0.125, INV_16 = 0.0625;
@@ -264,6 +266,12 @@ static void interp_zigzag_3d(const orc_grid* g, const real* EB, int i1, int i2,
         wp[a] = wpp[a];
       }
     }
+    /* reference quirk (sr.hpp:1100-1116): Bx3 reads the dual x2 stencil
+     * (j - 1 + indy, j + indy) but weights it with the primal ponpmy/ponppy */
+    if (c == 5) {
+      wm[1] = wpm[1];
+      wp[1] = wpp[1];
+    }
     const real c000 = EB[EBI(g, lo[0], lo[1], lo[2], c)];
     const real c100 = EB[EBI(g, lo[0] + 1, lo[1], lo[2], c)];
     const real c010 = EB[EBI(g, lo[0], lo[1] + 1, lo[2], c)];
@@ -305,9 +313,9 @@ static void interp_shape(const orc_grid* g, const real* EB, int O, const int* ic
       for (int b = 0; b < O + 1; b++) {
         real c0 = ZERO;
         for (int a = 0; a < O + 1; a++) {
-          c0 = RFMA(S[0][a], EB[EBI(g, mn[0] + a, mn[1] + b, 0, c)], c0);
+          c0 = IACC(S[0][a], EB[EBI(g, mn[0] + a, mn[1] + b, 0, c)], c0);
         }
-        v = RFMA(c0, S[1][b], v);
+        v = IACC(c0, S[1][b], v);
       }
     } else {
       for (int cc = 0; cc < O + 1; cc++) {
@@ -315,11 +323,11 @@ static void interp_shape(const orc_grid* g, const real* EB, int O, const int* ic
         for (int b = 0; b < O + 1; b++) {
           real c00 = ZERO;
           for (int a = 0; a < O + 1; a++) {
-            c00 = RFMA(S[0][a], EB[EBI(g, mn[0] + a, mn[1] + b, mn[2] + cc, c)], c00);
+            c00 = IACC(S[0][a], EB[EBI(g, mn[0] + a, mn[1] + b, mn[2] + cc, c)], c00);
           }
-          c0 = RFMA(c00, S[1][b], c0);
+          c0 = IACC(c00, S[1][b], c0);
         }
-        v = RFMA(c0, S[2][cc], v);
+        v = IACC(c0, S[2][cc], v);
       }
     }
     if (c < 3) e0[c] = v; else b0[c - 3] = v;

@@ -12,12 +12,10 @@
  * Arithmetic contract (shared with the CUDA kernels so results are bit-exact):
  *  - every operation is rounded separately in the reference's source order
  *    (the oracle is built with -ffp-contract=off, the CUDA code with
- *    -fmad=false);
- *  - the only fused multiply-adds are the running sums of the field
- *    interpolation at shape order >= 1 (`c += S * EB` in
- *    src/kernels/pushers/sr.hpp:1118-1369), evaluated as fma(S, EB, c) —
- *    the contraction nvcc applies by default to the reference's own CUDA
- *    build;
+ *    -fmad=false), including the running sums of the field interpolation
+ *    (`c += S * EB`, src/kernels/pushers/sr.hpp:1118-1369). This is the
+ *    arithmetic of the reference's own kernels compiled without contraction,
+ *    which tests/test_ref_pin.py checks against oracle/_ref;
  *  - current deposition differs from the GPU only in summation order.
  */
 #ifndef ENTITY_SRPIC_ORACLE_H

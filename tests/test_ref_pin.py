@@ -1,0 +1,311 @@
+"""The oracle against the reference's own code (CPU, no GPU).
+
+oracle/_ref holds Entity's SR kernels, its parameter derivation and its kernel
+tests, compiled unmodified from the reference sources against the host Kokkos
+shim (oracle/build_ref.py). These tests check:
+  * that the reference's own kernel tests (tests/kernels/*.cpp) pass against
+    the shim, in single and double precision;
+  * that the restated oracle (oracle/srpic_oracle.c) gives the same results
+    as the reference's kernels, bit for bit: push (2D/3D, orders 0-3, Boris,
+    Vay, photons, periodic/absorbing/reflecting walls), current deposit (every
+    particle's contribution and the summed J), Faraday (Yee and the extended
+    stencil), Ampere, CurrentsAmpere, the digital filter (including the 3D
+    duplicated term), the sort key, and 20 whole steps of plasmas shaped like
+    the 512^2 pair plasma and the 256^3 turbulence box;
+  * that the C ABI's step scales (entity_gb300.sim.step_params) equal the
+    reference's TOML-to-scales derivation (parameters.cpp:47-78,
+    algorithms.cpp:18-27, grid.cpp:510-574).
+The GPU tests compare the CUDA path with the oracle, so these pins carry over.
+
+Skipped when the reference checkout is absent (the GPU machine has none).
+"""
+import ctypes as C
+import subprocess
+
+import pytest
+import torch
+
+from entity_gb300.inputs import GridSpec, empty_field, make_species
+from entity_gb300.sim import step_params
+from oracle import build_ref
+from oracle.oracle import Oracle
+from tests.helpers import random_currents, random_fields
+
+pytestmark = pytest.mark.skipif(not build_ref.reference_root(),
+                                reason="the reference checkout is not available")
+
+REALS = [torch.float32, torch.float64]
+
+
+def _ref(g):
+    from oracle.ref import RefOracle
+    return RefOracle(g)
+
+
+def _grid(dim, order, real, **kw):
+    n = (32, 24, 1) if dim == 2 else (12, 10, 8)
+    return GridSpec(dim=dim, n=n, order=order, real=real, **kw)
+
+
+def _assert_species_equal(a, b, dim):
+    for d in range(dim):
+        assert torch.equal(a.i[d], b.i[d]), f"i{d + 1}"
+        assert torch.equal(a.dx[d], b.dx[d]), f"dx{d + 1}"
+        assert torch.equal(a.i_prev[d], b.i_prev[d]), f"i{d + 1}_prev"
+        assert torch.equal(a.dx_prev[d], b.dx_prev[d]), f"dx{d + 1}_prev"
+    for d in range(3):
+        assert torch.equal(a.u[d], b.u[d]), f"u{d + 1}"
+    assert torch.equal(a.tag, b.tag)
+
+
+@pytest.mark.parametrize("tag", ["f32", "f64"])
+@pytest.mark.parametrize("name", build_ref.KERNEL_TESTS)
+def test_reference_kernel_tests_pass_on_the_shim(name, tag):
+    exe = build_ref.build_tests()[(name, tag)]
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+
+
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("order", [0, 1, 2, 3])
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("pusher", [1, 2])
+def test_push_matches_reference(dim, order, real, pusher):
+    g = _grid(dim, order, real)
+    EB = random_fields(g, 11 + dim * 10 + order)
+    sp = make_species(g, 4, 0.5, 0.3, 100 + order, pusher=pusher)
+    a, b = sp.clone(), sp.clone()
+    _ref(g).push(a, EB, 0.45, 0.7, g.dx)
+    assert Oracle(g).push(b, EB, 0.45, 0.7, g.dx) == 0
+    _assert_species_equal(b, a, dim)
+
+
+@pytest.mark.parametrize("real", REALS)
+def test_photon_push_matches_reference(real):
+    g = _grid(3, 2, real)
+    EB = random_fields(g, 3)
+    sp = make_species(g, 4, 1.0, 0.0, 4, pusher=3, mass=0.0, charge=0.0)
+    a, b = sp.clone(), sp.clone()
+    _ref(g).push(a, EB, 0.4, 1.0, g.dx)
+    Oracle(g).push(b, EB, 0.4, 1.0, g.dx)
+    _assert_species_equal(b, a, 3)
+
+
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("bc", [1, 2])
+def test_wall_push_matches_reference(bc, dim, real):
+    # absorbing (1) or reflecting (2) walls on x1, periodic elsewhere
+    n = (16, 16, 1) if dim == 2 else (10, 8, 8)
+    g = GridSpec(dim=dim, n=n, order=1, real=real, periodic=(0, 1, 1),
+                 prtl_bc=((bc, bc), (0, 0), (0, 0)))
+    EB = random_fields(g, 5)
+    sp = make_species(g, 8, 1.0, 0.0, 9)
+    a, b = sp.clone(), sp.clone()
+    _ref(g).push(a, EB, 0.6, 0.5, g.dx)
+    Oracle(g).push(b, EB, 0.6, 0.5, g.dx)
+    _assert_species_equal(b, a, dim)
+    if bc == 1:
+        assert int((a.tag == 0).sum()) > 0
+
+
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("order", [0, 1, 2, 3])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_deposit_matches_reference(dim, order, real):
+    g = _grid(dim, order, real)
+    EB = random_fields(g, 21)
+    sp = make_species(g, 4, 0.5, 0.3, 200 + order)
+    o, r = Oracle(g), _ref(g)
+    o.push(sp, EB, 0.45, 0.7, g.dx)          # sets the prev arrays
+    Jr, Jo = empty_field(g, 3), empty_field(g, 3)
+    r.deposit([sp], Jr, 0.45, g.dx)
+    o.deposit([sp], Jo, 0.45, g.dx)
+    # same particle partition and summation order on both sides: exact
+    assert torch.equal(Jo, Jr)
+    # and every particle's own contribution, Esirkepov's 3D THIRD weights
+    # and the zigzag relay point included
+    for k in range(0, sp.npart, max(1, sp.npart // 48)):
+        one = sp.clone()
+        for lst in (one.i, one.dx, one.i_prev, one.dx_prev, one.u):
+            for d in range(len(lst)):
+                lst[d] = lst[d][k:k + 1].clone()
+        one.w, one.tag, one.npart = one.w[k:k + 1].clone(), one.tag[k:k + 1].clone(), 1
+        Jr.zero_()
+        Jo.zero_()
+        r.deposit([one], Jr, 0.45, g.dx)
+        o.deposit([one], Jo, 0.45, g.dx)
+        assert torch.equal(Jo, Jr), k
+
+
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("dim", [2, 3])
+def test_field_kernels_match_reference(dim, real):
+    g = _grid(dim, 2, real)
+    o, r = Oracle(g), _ref(g)
+    ext = [0.05, 0.04, 0.02, 0.03, 0.01, 0.02, 0.015, 0.025, 0.005]
+    for stencil in (None, ext):
+        a = random_fields(g, 31)
+        b = a.clone()
+        r.faraday(a, 0.21, 0.13, stencil)
+        o.faraday(b, 0.21, 0.13, stencil)
+        assert torch.equal(a, b), "Faraday"
+    a = random_fields(g, 32)
+    b = a.clone()
+    r.ampere(a, 0.33, 0.11)
+    o.ampere(b, 0.33, 0.11)
+    assert torch.equal(a, b), "Ampere"
+    a, b = random_fields(g, 33), None
+    b = a.clone()
+    ja = random_currents(g, 34)
+    jb = ja.clone()
+    r.currents_ampere(a, ja, -0.02, 8.0)
+    o.currents_ampere(b, jb, -0.02, 8.0)
+    assert torch.equal(a, b) and torch.equal(ja, jb), "CurrentsAmpere"
+    ja = random_currents(g, 35)
+    jb = ja.clone()
+    for _ in range(3):
+        r.filter_pass(ja, empty_field(g, 3))
+        o.filter_pass(jb, empty_field(g, 3))
+    assert torch.equal(ja, jb), "DigitalFilter"
+
+
+def test_3d_filter_quirk_is_the_references():
+    # one pass over a unit spike: the reference's 27-point stencil repeats
+    # (i, j, k+-1) in its 1/32 group (digital_filter.hpp:365), so the z faces
+    # weigh 3/32 and the (0, +-1, -+1) edges nothing
+    g = GridSpec(dim=3, n=(8, 8, 8), order=1, real=torch.float64)
+    J = empty_field(g, 3)
+    ng = g.ng
+    J[0, ng + 4, ng + 4, ng + 4] = 1.0
+    _ref(g).filter_pass(J, empty_field(g, 3))
+    c = J[0, ng + 3:ng + 6, ng + 3:ng + 6, ng + 3:ng + 6]   # (k, j, i)
+    assert float(c[0, 1, 1]) == pytest.approx(3 / 32) and float(c[2, 1, 1]) == pytest.approx(3 / 32)
+    assert float(c[0, 2, 1]) == 0.0 and float(c[2, 0, 1]) == 0.0
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_sort_key_matches_reference(dim):
+    g = _grid(dim, 1, torch.float32)
+    sp = make_species(g, 5, 0.1, 0.0, 7)
+    sp.tag[::7] = 0
+    keys = _ref(g).sort_keys(sp)
+    ncell = g.ncells()
+    alive = sp.tag == 1
+    # dead particles get total_tiles + 1 (sorting.h:119-121)
+    assert bool((keys[~alive] == ncell + 1).all())
+    if dim == 2:
+        mine = sp.i[0].long() * g.n[1] + sp.i[1].long()
+    else:
+        mine = (sp.i[0].long() * g.n[1] + sp.i[1].long()) * g.n[2] + sp.i[2].long()
+    assert torch.equal(keys[alive], mine[alive])
+    # the oracle's sort orders the particles by that key, stably, dead last
+    perm = Oracle(g).sort(sp)
+    k = keys[perm]
+    assert bool((k[1:] >= k[:-1]).all())
+    same = k[1:] == k[:-1]
+    assert bool((perm[1:][same] > perm[:-1][same]).all())
+
+
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("shape", ["pair2d", "turb3d"])
+def test_steps_match_reference(shape, real):
+    # 20 whole steps (srpic.hpp:65-188) with the reference's kernels against
+    # the oracle's: identical particles, fields and currents after every step
+    if shape == "pair2d":
+        g = GridSpec(dim=2, n=(32, 32, 1), order=1, real=real)
+        prm = step_params(g, cfl=0.45, ppc0=32.0, skindepth0=10.0, larmor0=10.0, nfilter=0,
+                          sort_interval=8, write_prev=True)
+        e = make_species(g, 16, 0.01, 0.3, 1, charge=-1.0)
+        p = make_species(g, 16, 0.01, -0.3, 2, charge=1.0, index=2)
+        EB = empty_field(g, 6)
+    else:
+        g = GridSpec(dim=3, n=(16, 16, 16), order=2, real=real)
+        prm = step_params(g, cfl=0.45, ppc0=16.0, skindepth0=10.0, larmor0=10.0, nfilter=4,
+                          sort_interval=8, write_prev=True)
+        e = make_species(g, 8, 0.09, 0.0, 3, charge=-1.0)
+        p = make_species(g, 8, 0.09, 0.0, 4, charge=1.0, index=2)
+        EB = random_fields(g, 5, amp=0.1)
+    o, r = Oracle(g), _ref(g)
+    so, sr = [e.clone(), p.clone()], [e.clone(), p.clone()]
+    Eo, Er = EB.clone(), EB.clone()
+    Jo, Jr = empty_field(g, 3), empty_field(g, 3)
+    Bo, Br = empty_field(g, 3), empty_field(g, 3)
+    for step in range(20):
+        o.step(so, Eo, Jo, Bo, prm, step)
+        r.step(sr, Er, Jr, Br, prm, step)
+        assert torch.equal(Eo, Er), step
+        assert torch.equal(Jo, Jr), step
+        for a, b in zip(so, sr):
+            _assert_species_equal(a, b, g.dim)
+
+
+_TOML = """
+[simulation]
+name = "pin"
+engine = "srpic"
+runtime = 1.0
+[grid]
+resolution = {res}
+extent = {ext}
+[grid.metric]
+metric = "minkowski"
+[grid.boundaries]
+fields = {bnd}
+particles = {bnd}
+[scales]
+larmor0 = {larmor0}
+skindepth0 = {skindepth0}
+[algorithms]
+current_filters = 4
+[algorithms.timestep]
+CFL = {cfl}
+[particles]
+ppc0 = {ppc0}
+[[particles.species]]
+label = "e-"
+mass = 1.0
+charge = -1.0
+maxnpart = 1e3
+[output]
+format = "disabled"
+"""
+
+
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("case", [
+    dict(dim=2, n=(512, 512), L=512.0, cfl=0.45, ppc0=32.0, skindepth0=10.0, larmor0=10.0),
+    dict(dim=3, n=(256, 256, 256), L=256.0, cfl=0.45, ppc0=16.0, skindepth0=10.0,
+         larmor0=10.0),
+    dict(dim=3, n=(192, 192, 192), L=96.0, cfl=0.45, ppc0=64.0, skindepth0=10.0,
+         larmor0=3.1622776601683795),
+    dict(dim=2, n=(48, 32), L=7.5, cfl=0.9, ppc0=5.0, skindepth0=0.7, larmor0=0.3),
+])
+def test_step_scales_match_reference(case, real):
+    # the scales the C ABI takes, derived by entity_gb300.sim.step_params,
+    # against the reference's own TOML-to-scales code on the same inputs
+    tag = "f32" if real == torch.float32 else "f64"
+    L = C.CDLL(build_ref.build()[("params", tag)])
+    L.ref_scales.argtypes = [C.c_char_p, C.POINTER(C.c_double), C.c_char_p, C.c_int]
+    L.ref_scales.restype = C.c_int
+    dim, n = case["dim"], case["n"]
+    dx = case["L"] / n[0]
+    text = _TOML.format(res=list(n), ext=[[0.0, dx * k] for k in n],
+                        bnd=[["PERIODIC"]] * dim, larmor0=case["larmor0"],
+                        skindepth0=case["skindepth0"], cfl=case["cfl"], ppc0=case["ppc0"])
+    out = (C.c_double * 10)()
+    err = C.create_string_buffer(4096)
+    assert L.ref_scales(text.encode(), out, err, 4096) == 0, err.value.decode()
+    dt, dx0, V0, n0, q0, B0, omegaB0, corr, ppc0, sigma0 = list(out)
+    g = GridSpec(dim=dim, n=tuple(n) + ((1,) if dim == 2 else ()), order=1, real=real,
+                 extent=case["L"])
+    prm = step_params(g, cfl=case["cfl"], ppc0=case["ppc0"], skindepth0=case["skindepth0"],
+                      larmor0=case["larmor0"])
+    assert prm.dt == dt
+    assert prm.V0 == V0
+    assert prm.q0 == q0
+    assert prm.B0 == B0
+    assert prm.omegaB0 == omegaB0
+    assert prm.correction == corr
+    assert prm.ppc0 == ppc0
+    assert prm.dx == float(torch.tensor(case["L"], dtype=real) / float(n[0]))
