@@ -60,9 +60,10 @@ def _assert_species_equal(a, b, dim):
 
 @pytest.mark.parametrize("tag", ["f32", "f64"])
 @pytest.mark.parametrize("name", build_ref.KERNEL_TESTS)
-def test_reference_kernel_tests_pass_on_the_shim(name, tag):
+def test_reference_kernel_tests_pass_on_the_shim(name, tag, tmp_path):
     exe = build_ref.build_tests()[(name, tag)]
-    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    # some write logs into their working directory
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600, cwd=tmp_path)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
 
 
