@@ -43,12 +43,13 @@ WORKLOADS = {
                         "4 filter passes, FP32", dim=3, n=(256, 256, 256), order=2, ppc=8,
                    temp=0.09, drift=0.0, nfilter=4, cfl=0.45, skindepth0=10.0, larmor0=10.0,
                    ppc0=16.0, field="turbulent", modes=8, dB=1.0, sample_n=(64, 64, 64),
-                   precision_n=(64, 64, 64), precision_steps=200, sort_interval=8,
-                   bench_steps=8),
+                   reference_n=(128, 128, 128), precision_n=(64, 64, 64),
+                   precision_steps=200, sort_interval=8, bench_steps=8),
     "pair2d": dict(name="2D SR pair plasma 512^2, e-/e+ 16 ppc each, drift +-0.3c, order 1, FP32",
                    dim=2, n=(512, 512, 1), order=1, ppc=16, temp=0.01, drift=0.3, nfilter=0,
                    cfl=0.45, skindepth0=10.0, larmor0=10.0, ppc0=16.0, field="none", modes=0,
-                   dB=0.0, sample_n=(128, 128, 1), precision_n=(512, 512, 1),
+                   dB=0.0, sample_n=(128, 128, 1), reference_n=(512, 512, 1),
+                   precision_n=(512, 512, 1),
                    precision_steps=100, sort_interval=16, bench_steps=16),
     # magnetized uniform plasma: sigma = (skin depth / Larmor radius)^2 = 10,
     # Maxwell-Juttner theta = 1, uniform B0 along x3
@@ -81,7 +82,8 @@ WORKLOADS = {
                          "theta 1, order 3, FP32 vs FP64", dim=3, n=(192, 192, 192), order=3,
                     ppc=32, temp=1.0, drift=0.0, nfilter=0, cfl=0.45, skindepth0=10.0,
                     larmor0=10.0 / math.sqrt(10.0), ppc0=64.0, field="uniform", modes=0, dB=0.0,
-                    sample_n=(24, 24, 24), precision_n=(192, 192, 192), precision_steps=1000,
+                    sample_n=(24, 24, 24), reference_n=(48, 48, 48),
+                    precision_n=(192, 192, 192), precision_steps=1000,
                     sort_interval=4),
 }
 
@@ -208,15 +210,18 @@ def hbm_peak():
     return 6800.0, "fallback"
 
 
-def cpu_sample(w, steps, warmup=1):
-    """The oracle (CPU restatement of the reference step, OpenMP over all host
-    cores) on a sub-box of the workload with the same per-cell content."""
+def cpu_sample(w, steps, warmup=1, n=None, sort_interval=0):
+    """The oracle (the CPU restatement of the reference step, bit-exact with
+    the reference's own kernels, OpenMP over all host cores) on a sub-box of
+    the workload with the same per-cell content; with sort_interval > 0 it
+    sorts by the reference's cell key as often as the GPU arm sorts."""
     from oracle.oracle import Oracle, lib
-    g, EB, J, buff, sp = make_setup(w, "cpu", n=w["sample_n"])
+    n = n or w["sample_n"]
+    g, EB, J, buff, sp = make_setup(w, "cpu", n=n)
     for s in sp:
         s.i_prev = [x.clone() for x in s.i]
         s.dx_prev = [x.clone() for x in s.dx]
-    prm = step_prm(g, w, 0)
+    prm = step_prm(g, w, sort_interval)
     o = Oracle(g)
     threads = lib(g.real).orc_max_threads()
     for k in range(warmup):
@@ -226,10 +231,36 @@ def cpu_sample(w, steps, warmup=1):
         o.step(sp, EB, J, buff, prm, warmup + k)
     dt = time.perf_counter() - t0
     npart = sum(s.npart for s in sp)
+    sort = f"sort every {sort_interval} steps" if sort_interval else "sort off"
     return {"value": npart * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": (f"{'x'.join(str(v) for v in w['sample_n'][:w['dim']])} cells of the same "
+            "host_cpus": len(os.sched_getaffinity(0)),
+            "sample": (f"{'x'.join(str(v) for v in n[:w['dim']])} cells of the same "
                        f"plasma ({npart} particles), {steps} full steps after {warmup} warm-up, "
-                       f"sort off"), "seconds": dt}
+                       f"{sort}"), "seconds": dt}
+
+
+def repo_libraries_mapped():
+    """The shared libraries of this repository that the process has mapped."""
+    libs = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if len(line.split()) >= 6 else ""
+                if path.startswith(ROOT) and ".so" in path:
+                    libs.add(os.path.relpath(path, ROOT))
+    except OSError:
+        return None
+    return sorted(libs)
+
+
+def workload_config(w, args, ncells, npart, world):
+    """The config of a bench line, the same for both arms."""
+    # i, dx (4 B per axis each), u (3 x 4 B), w (4 B) and the 2-byte tag
+    state = npart * (8 * w["dim"] + 18)
+    return {"workload": w["name"], "cells": ncells, "particles_per_gpu": npart,
+            "sort_interval": args.sort_interval,
+            "l2": f"inputs larger than L2 (particle state {state / 1e9:.2f} GB)",
+            "parallelism": f"replicas x{world}"}
 
 
 def precision_twin(w, n, steps, sort_interval, every, timers=False, warm=0):
@@ -303,20 +334,30 @@ def precision_twin(w, n, steps, sort_interval, every, timers=False, warm=0):
 
 
 def run_reference(args, w):
+    """The reference's algorithm on the host cores: the oracle, which is
+    bit-exact with the reference's own kernels (tests/test_ref_pin.py). Only
+    the oracle is built and loaded here; the product library is not."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from __graft_entry__ import build
-    build()
-    base = cpu_sample(w, steps=args.steps, warmup=args.warmup)
+    from oracle import build_oracle
+    build_oracle.build()
+    n_full = args.cells or w["n"]
+    full_cells = math.prod(n_full[:w["dim"]])
+    full_npart = 2 * w["ppc"] * full_cells
+    base = cpu_sample(w, steps=args.steps, warmup=args.warmup, n=w["reference_n"],
+                      sort_interval=args.sort_interval)
     line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": base["seconds"] / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": w["name"], "sample": base["sample"]},
+            "ms_per_step": base["seconds"] / args.steps * 1e3 * full_npart /
+                           max(1, 2 * w["ppc"] * math.prod(w["reference_n"][:w["dim"]])),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": workload_config(w, args, full_cells, full_npart, 1),
             "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+                    "d2h_bytes_per_step": 0},
+            "libraries_mapped": repo_libraries_mapped()}
     print(json.dumps(line), flush=True)
 
 
@@ -431,11 +472,8 @@ def run_ours(args, w):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": w["name"], "cells": g.ncells(), "particles_per_gpu": npart,
-                   "sort_interval": args.sort_interval,
-                   "sort_key": "reference cell key" if args.reference_sort_key else "tile-major",
-                   "l2": "inputs larger than L2 (particle state > 10 GB per step)",
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(w, args, g.ncells(), npart, world),
+        "sort_key": "reference cell key" if args.reference_sort_key else "tile-major",
         "ns_per_particle_step": 1e9 / (value / world),
         "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in phases.items()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
