@@ -468,6 +468,11 @@ def run_ours(args, w):
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         cpu = cpu_sample(w, steps=args.cpu_steps)
+    # the metric's adjoint/forward ratio, on the two-stream adjoint problem
+    adj = None
+    if not args.no_adjoint and world == 1:
+        wa = WORKLOADS["adjoint2d"]
+        _, adj = adjoint_measure(wa, wa["steps"], wa["every"], wa["n"][:2], lib)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
@@ -488,23 +493,18 @@ def run_ours(args, w):
         "gpu_launches": launches,
         "clocks": clocks,
         "precision": precision,
+        "adjoint": adj,
     }
     print(json.dumps(line), flush=True)
 
 
-def run_adjoint(args, w):
-    """Adjoint/forward cost and gradient checks on the two-stream problem."""
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    from __graft_entry__ import build
-    build()
-    from entity_gb300 import abi
+def adjoint_measure(w, nsteps, every, n, lib, h_sweep=(1e-4, 3e-4, 1e-3, 2e-3, 4e-3)):
+    """Adjoint/forward cost and gradient checks on the two-stream problem:
+    FP32 forward and gradient timed with CUDA events, the FP64 gradient, and
+    central differences of both forwards at h = 1e-4 (the stated bar) and
+    over a sweep of h for the drift."""
     from entity_gb300 import adjoint as A
-    from entity_gb300.sim import Context, HostPipe
-    lib = abi.load()
-    nsteps = args.adjoint_steps or w["steps"]
-    every = args.checkpoint_every or w["every"]
-    n = (args.cells or w["n"])[:2]
+    from entity_gb300.sim import Context
 
     def setup(real):
         g, prm, kappa, k = A.two_stream(n=n, ppc_per_beam=w["ppc"], order=w["order"], real=real,
@@ -545,6 +545,7 @@ def run_adjoint(args, w):
             torch.cuda.synchronize()
             out["gradient_ms"] = e0.elapsed_time(e1)
         out.update(L=float(L.detach()), dL_dbeta=float(gb), dL_damp=float(ga))
+        ctx.close()
         return out
 
     def fd(real, which, h):
@@ -557,28 +558,51 @@ def run_adjoint(args, w):
                                     torch.tensor(a, dtype=torch.float64, device="cuda"), w["ppc"],
                                     ctx)
             vals.append(A.forward_energy(ctx, g, prm, sp, U, W, EB0, nsteps))
+        ctx.close()
         return (vals[0] - vals[1]) / (2 * h)
 
-    sampler = ClockSampler(local)
-    sampler.start()
     r32 = grads(torch.float32, timed=True)
-    clocks = sampler.stop()
     r64 = grads(torch.float64)
     rel = lambda a, b: abs(a - b) / abs(b) if b != 0 else abs(a - b)
-    # central differences at h = 1e-4, and for the drift also at 2e-3: the
-    # float in-cell offsets round every position each step (~3e-8 cells,
-    # coherently across a cold beam), which a 1e-4 drift change over 400
-    # steps resolves only to ~1e-3
-    checks = {"h": 1e-4, "h_drift_large": 2e-3}
+    # central differences at h = 1e-4 (the stated bar). The in-cell offsets
+    # are float at every precision and a cold beam rounds them coherently
+    # (~3e-8 cells per step), so the difference quotient of the drift
+    # resolves dL/dbeta only to ~1e-3 at h = 1e-4; the sweep over h shows it
+    checks = {"h": 1e-4}
     for real, tag, r in ((torch.float32, "f32", r32), (torch.float64, "f64", r64)):
-        fb, fa, fb2 = fd(real, "beta", 1e-4), fd(real, "amp", 1e-4), fd(real, "beta", 2e-3)
+        fb, fa = fd(real, "beta", 1e-4), fd(real, "amp", 1e-4)
         checks[tag] = {"dL_dbeta": r["dL_dbeta"], "fd_dbeta": fb,
                        "rel_err_dbeta": rel(r["dL_dbeta"], fb),
-                       "fd_dbeta_h2e-3": fb2, "rel_err_dbeta_h2e-3": rel(r["dL_dbeta"], fb2),
                        "dL_damp": r["dL_damp"], "fd_damp": fa, "rel_err_damp": rel(r["dL_damp"], fa)}
+    checks["f64_dbeta_h_sweep"] = [
+        {"h": h, "fd_dbeta": v, "rel_err_vs_f64_adjoint": rel(r64["dL_dbeta"], v)}
+        for h, v in ((h, fd(torch.float64, "beta", h)) for h in h_sweep)]
     checks["f32_vs_f64"] = {"rel_err_dbeta": rel(r32["dL_dbeta"], r64["dL_dbeta"]),
                             "rel_err_damp": rel(r32["dL_damp"], r64["dL_damp"]),
                             "rel_err_L": rel(r32["L"], r64["L"])}
+    return r32, {"ratio_gradient_to_forward": r32["gradient_ms"] / r32["forward_ms"],
+                 "forward_ms": r32["forward_ms"], "gradient_ms": r32["gradient_ms"],
+                 "gradient_first_ms": r32["gradient_first_ms"], "steps": nsteps,
+                 "checkpoint_every": every, "particles": r32["particles"],
+                 "L": r32["L"], "L_forward": r32["L_forward"], "checks": checks,
+                 "workload": w["name"]}
+
+
+def run_adjoint(args, w):
+    """Adjoint/forward cost and gradient checks on the two-stream problem."""
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from __graft_entry__ import build
+    build()
+    from entity_gb300 import abi
+    lib = abi.load()
+    nsteps = args.adjoint_steps or w["steps"]
+    every = args.checkpoint_every or w["every"]
+    n = (args.cells or w["n"])[:2]
+    sampler = ClockSampler(local)
+    sampler.start()
+    r32, adj = adjoint_measure(w, nsteps, every, n, lib)
+    clocks = sampler.stop()
     npart = r32["particles"]
     value = npart * nsteps / (r32["forward_ms"] / 1e3)
     line = {
@@ -588,10 +612,7 @@ def run_adjoint(args, w):
         "data": "synthetic",
         "config": {"workload": w["name"], "cells": n[0] * n[1], "particles_per_gpu": npart,
                    "checkpoint_every": every, "sort_interval": 0, "parallelism": "replicas x1"},
-        "adjoint": {"ratio_gradient_to_forward": r32["gradient_ms"] / r32["forward_ms"],
-                    "forward_ms": r32["forward_ms"], "gradient_ms": r32["gradient_ms"],
-                    "gradient_first_ms": r32["gradient_first_ms"],
-                    "L": r32["L"], "L_forward": r32["L_forward"], "checks": checks},
+        "adjoint": adj,
         "gpu_launches": r32["forward_launches"],
         "clocks": clocks,
     }
@@ -897,6 +918,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the two-stream adjoint block of the default line")
     ap.add_argument("--precision-steps", type=int, default=None,
                     help="steps of the FP32-vs-FP64 twin on the sub-box (0 = skip)")
     ap.add_argument("--checkpoint-every", type=int, default=None,
