@@ -69,6 +69,13 @@ class PicSpecies(C.Structure):
         ("charge", C.c_float),
         ("pusher", C.c_int32),
         ("index", C.c_int32),
+        ("phi", C.c_void_p),
+        ("pld_r", C.c_void_p),
+        ("pld_i", C.c_void_p),
+        ("pld_r_stride", C.c_int64 * 2),
+        ("pld_i_stride", C.c_int64 * 2),
+        ("npld_r", C.c_int32),
+        ("npld_i", C.c_int32),
     ]
 
 
@@ -220,6 +227,8 @@ SIGNATURES = {
                                          _VP]),
     "pic_gr_aux": (C.c_int, [_VP, C.POINTER(PicGRMetric), C.c_int32, _VP, _VP, _VP, _VP]),
     "pic_gr_average": (C.c_int, [_VP, C.c_int32, _VP, _VP, _VP]),
+    "pic_gr_filter_currents": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP, C.c_int32,
+                                         _VP]),
     "pic_gr_field_bcs": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, C.c_int32, C.c_int32,
                                    C.c_int32, _VP]),
     "pic_gr_init_vertical": (C.c_int, [_VP, C.POINTER(PicGRMetric), _VP, _VP]),

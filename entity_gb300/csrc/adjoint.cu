@@ -462,7 +462,7 @@ template <typename real>
 cudaError_t launch_push_deposit_adjoint(int order, const AdjArgs<real>& a, cudaStream_t s) {
   if (a.sp.npart <= 0) return cudaSuccess;
   int64_t blocks = (a.sp.npart + 255) / 256;
-  if (blocks > 152 * 32) blocks = 152 * 32;
+  if (blocks > pic::sm_count() * 32) blocks = pic::sm_count() * 32;
   const unsigned g = (unsigned)blocks;
   switch (order) {
     case 1: PIC_KL(k_push_deposit_adjoint<1, real><<<g, 256, 0, s>>>(a)); break;

@@ -110,6 +110,12 @@ inline int validate_species(const pic_ctx* c, const pic_species* sp, bool need_p
     if (c->grid.dim == 3 && (!sp->i3_prev || !sp->dx3_prev)) return PIC_ERR_ARG;
   }
   if (sp->pusher < PIC_PUSHER_NONE || sp->pusher > PIC_PUSHER_PHOTON) return PIC_ERR_ARG;
+  // payload columns: a base pointer and positive strides when present
+  if (sp->npld_r < 0 || sp->npld_i < 0) return PIC_ERR_ARG;
+  if (sp->npld_r > 0 && (!sp->pld_r || sp->pld_r_stride[0] < 1 || sp->pld_r_stride[1] < 1))
+    return PIC_ERR_ARG;
+  if (sp->npld_i > 0 && (!sp->pld_i || sp->pld_i_stride[0] < 1 || sp->pld_i_stride[1] < 1))
+    return PIC_ERR_ARG;
   return PIC_OK;
 }
 

@@ -248,7 +248,7 @@ cudaError_t launch_filter_cond(const GridInfo& g, const int lo[3], const int hi[
   for (int d = 0; d < 3; ++d) cf.lo[d] = lo[d], cf.hi[d] = hi[d];
   const int64_t cnt = (int64_t)g.n[0] * g.n[1] * (g.dim == 3 ? g.n[2] : 1);
   int64_t       nb  = (cnt + 255) / 256;
-  if (nb > 152 * 64) nb = 152 * 64;
+  if (nb > pic::sm_count() * 64) nb = pic::sm_count() * 64;
   if (g.dim == 2) PIC_KL(k_filter_cond<2, real><<<(unsigned)nb, 256, 0, s>>>(g, cf, buff, J));
   else            PIC_KL(k_filter_cond<3, real><<<(unsigned)nb, 256, 0, s>>>(g, cf, buff, J));
   return cudaGetLastError();
@@ -265,7 +265,7 @@ namespace {
 
 unsigned blocks(int64_t n) {
   int64_t b = (n + 255) / 256;
-  if (b > 152 * 32) b = 152 * 32;
+  if (b > pic::sm_count() * 32) b = pic::sm_count() * 32;
   return (unsigned)(b < 1 ? 1 : b);
 }
 

@@ -76,7 +76,7 @@ CellIter make_iter(const GridInfo& g) {
 
 dim3 grid_for(int64_t count, int threads) {
   int64_t b = (count + threads - 1) / threads;
-  if (b > 152 * 128) b = 152 * 128;
+  if (b > pic::sm_count() * 128) b = pic::sm_count() * 128;
   if (b < 1) b = 1;
   return dim3((unsigned)b);
 }
@@ -629,7 +629,7 @@ cudaError_t launch_energy(const GridInfo& g, FieldView<real> EB, double dx, doub
                           cudaStream_t s) {
   const CellIter it = make_iter(g);
   int64_t        b  = (it.count + 255) / 256;
-  if (b > 152 * 8) b = 152 * 8;
+  if (b > pic::sm_count() * 8) b = pic::sm_count() * 8;
   if (g.dim == 2) PIC_KL(k_energy<2, real><<<(unsigned)b, 256, 0, s>>>(it, EB, dx, out));
   else            PIC_KL(k_energy<3, real><<<(unsigned)b, 256, 0, s>>>(it, EB, dx, out));
   return cudaGetLastError();

@@ -571,6 +571,70 @@ __global__ void k_gr_average(Range2 R, FieldView<real> a, FieldView<real> b, int
   }
 }
 
+// one pass of grpic::CurrentsFilter (src/engines/grpic/currents.h:74-101):
+// DigitalFilter_kernel's 2D non-Cartesian branch (digital_filter.hpp:196-276)
+// writes A from the copy B over i1 in [ng, ng + n1), i2 in [ng, ng + n2]
+// (the range runs over the upper axis row); the rows next to an axis take the
+// reference's one-sided theta weights, in its operation order
+template <typename real>
+__global__ void k_gr_filter(GRFld<real> f, Range2 R, FieldView<real> A, FieldView<real> B) {
+  const real ZERO = 0, INV_2 = 0.5, INV_4 = 0.25, INV_8 = 0.125, INV_16 = 0.0625;
+  const int  i2min = f.ng, i2max = f.n2 + f.ng;
+#define BB(a, b, c) B.p[B.idx(a, b, 0, c)]
+#define F1(c, a, b) (INV_2 * BB(a, b, c) + INV_4 * (BB((a) - 1, b, c) + BB((a) + 1, b, c)))
+  GR_CELL_LOOP(R)
+    real c00, c0p1, c0m1;
+    if (f.axis_min && i2 == i2min) {
+      c00  = F1(0, i1, i2);
+      c0p1 = F1(0, i1, i2 + 1);
+      A.p[A.idx(i1, i2, 0, 0)] = INV_2 * c00 + INV_2 * c0p1;
+      A.p[A.idx(i1, i2, 0, 2)] = ZERO;
+      c00  = F1(1, i1, i2);
+      c0p1 = F1(1, i1, i2 + 1);
+      A.p[A.idx(i1, i2, 0, 1)] = INV_4 * (c00 + c0p1);
+    } else if (f.axis_min && i2 == i2min + 1) {
+      c00  = F1(0, i1, i2);
+      c0p1 = F1(0, i1, i2 + 1);
+      c0m1 = F1(0, i1, i2 - 1);
+      A.p[A.idx(i1, i2, 0, 0)] = INV_2 * c00 + INV_4 * (c0p1 + c0m1);
+      c00  = F1(2, i1, i2);
+      c0p1 = F1(2, i1, i2 + 1);
+      A.p[A.idx(i1, i2, 0, 2)] = INV_2 * c00 + INV_4 * c0p1;
+      c00  = F1(1, i1, i2);
+      c0p1 = F1(1, i1, i2 + 1);
+      c0m1 = F1(1, i1, i2 - 1);
+      A.p[A.idx(i1, i2, 0, 1)] = INV_2 * c00 + INV_4 * (c0m1 + c0p1);
+    } else if (f.axis_max && i2 == i2max - 1) {
+      c00  = F1(0, i1, i2);
+      c0p1 = F1(0, i1, i2 + 1);
+      c0m1 = F1(0, i1, i2 - 1);
+      A.p[A.idx(i1, i2, 0, 0)] = INV_2 * c00 + INV_4 * (c0m1 + c0p1);
+      c00  = F1(2, i1, i2);
+      c0m1 = F1(2, i1, i2 - 1);
+      A.p[A.idx(i1, i2, 0, 2)] = INV_2 * c00 + INV_4 * c0m1;
+      c00  = F1(1, i1, i2);
+      c0m1 = F1(1, i1, i2 - 1);
+      A.p[A.idx(i1, i2, 0, 1)] = INV_4 * (c00 + c0m1);
+    } else if (f.axis_max && i2 == i2max) {
+      c00  = F1(0, i1, i2);
+      c0m1 = F1(0, i1, i2 - 1);
+      A.p[A.idx(i1, i2, 0, 0)] = INV_2 * c00 + INV_2 * c0m1;
+      A.p[A.idx(i1, i2, 0, 2)] = ZERO;
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        A.p[A.idx(i1, i2, 0, c)] =
+          INV_4 * BB(i1, i2, c) +
+          INV_8 * (BB(i1 - 1, i2, c) + BB(i1 + 1, i2, c) + BB(i1, i2 - 1, c) + BB(i1, i2 + 1, c)) +
+          INV_16 * (BB(i1 - 1, i2 - 1, c) + BB(i1 + 1, i2 + 1, c) + BB(i1 - 1, i2 + 1, c) +
+                    BB(i1 + 1, i2 - 1, c));
+      }
+    }
+  }
+#undef F1
+#undef BB
+}
+
 // AxisBoundaries_kernel (fields_bcs.hpp:825-868), per i1 over all cells
 template <typename real>
 __global__ void k_gr_axis(GRFld<real> f, FieldView<real> F, int set_e, int set_b) {
@@ -768,7 +832,7 @@ pic::GRFld<real> fld_of(const pic_ctx* c, const pic_gr_metric* g) {
 
 unsigned blocks_for(int64_t n) {
   int64_t b = (n + 255) / 256;
-  if (b > 152 * 64) b = 152 * 64;
+  if (b > pic::sm_count() * 64) b = pic::sm_count() * 64;
   return (unsigned)(b < 1 ? 1 : b);
 }
 
@@ -895,7 +959,7 @@ int gr_push_species(pic_ctx* c, const pic_gr_metric* g, const pic_species* const
     if (cudaStreamWaitEvent(s2, c->gr_fork, 0) != cudaSuccess) return PIC_ERR_CUDA;
     if constexpr (sizeof(real) == 4) {
       // three 128-thread blocks per SM fit at up to 170 registers per thread
-      const unsigned bi = 152 * 3;
+      const unsigned bi = (unsigned)pic::sm_count() * 3;
       switch (c->grid.order) {
         case 1: PIC_KL(pic::k_gr_push_island<1, real><<<bi, 128, 0, s2>>>(a[k])); break;
         case 2: PIC_KL(pic::k_gr_push_island<2, real><<<bi, 128, 0, s2>>>(a[k])); break;
@@ -1148,6 +1212,36 @@ int pic_gr_average(pic_ctx* c, int32_t which, void* a, void* b, void* stream) {
   return cuda_status(cudaGetLastError());
 }
 
+int pic_gr_filter_currents(pic_ctx* c, const pic_gr_metric* g, void* J, void* buff,
+                           int32_t npasses, void* stream) {
+  int st = gr_check(c, g);
+  if (st != PIC_OK) return st;
+  if (!J || !buff || npasses < 0 || J == buff) return PIC_ERR_ARG;
+  if (npasses == 0) return PIC_OK;
+  cudaStream_t      s  = strm(stream);
+  const int         ng = c->grid.ng;
+  const pic::Range2 R{ ng, c->grid.n[0] + ng, ng, c->grid.n[1] + ng + 1 };
+  const unsigned    b = blocks_for(R.count());
+  // bytes spanned by a 3-component field with the cur strides
+  int64_t span = 2 * c->grid.cur_stride[3];
+  for (int d = 0; d < 2; ++d) span += (int64_t)(c->grid.n[d] + 2 * ng - 1) * c->grid.cur_stride[d];
+  const size_t bytes = (size_t)(span + 1) * (size_t)c->grid.real_bytes;
+  for (int k = 0; k < npasses; ++k) {
+    // buff <- cur0 (currents.h:90), then the stencil back into cur0
+    if (cudaMemcpyAsync(buff, J, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return PIC_ERR_CUDA;
+    if (is_f64(c)) {
+      PIC_KL(pic::k_gr_filter<double><<<b, 256, 0, s>>>(fld_of<double>(c, g), R, cur_view<double>(c, J),
+                                                        cur_view<double>(c, buff)));
+    } else {
+      PIC_KL(pic::k_gr_filter<float><<<b, 256, 0, s>>>(fld_of<float>(c, g), R, cur_view<float>(c, J),
+                                                       cur_view<float>(c, buff)));
+    }
+    if (cudaGetLastError() != cudaSuccess) return PIC_ERR_CUDA;
+  }
+  return PIC_OK;
+}
+
 int pic_gr_field_bcs(pic_ctx* c, const pic_gr_metric* g, void* fld, int32_t set_e, int32_t set_b,
                      int32_t nfilter, void* stream) {
   int st = gr_check(c, g);
@@ -1225,7 +1319,7 @@ int pic_gr_min_cell_size(pic_ctx* c, const pic_gr_metric* g, double* out, void* 
   if (st != PIC_OK) return st;
   if (!out) return PIC_ERR_ARG;
   cudaStream_t s  = strm(stream);
-  const int    nb = 152;
+  const int    nb = pic::sm_count();
   double*      d  = nullptr;
   if (cudaMallocAsync((void**)&d, sizeof(double) * nb, s) != cudaSuccess) return PIC_ERR_NOMEM;
   const QKS<double> m = is_f64(c) ? make_qks<double>(c, g) : make_qks<float>(c, g);

@@ -331,7 +331,7 @@ int inject(pic_ctx* c, const pic_gr_metric* gm, pic_species* sp1, pic_species* s
   *n_pairs = n;
   if (n == 0) return PIC_OK;
   int64_t b = (n + 255) / 256;
-  if (b > 152 * 32) b = 152 * 32;
+  if (b > pic::sm_count() * 32) b = pic::sm_count() * 32;
   if (gm) {
     PIC_KL(pic::k_inject_uniform<2, true, real><<<(unsigned)b, 256, 0, s>>>(a));
   } else if (D == 2) {

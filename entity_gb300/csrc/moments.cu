@@ -116,7 +116,7 @@ cudaError_t launch_charge_density(int dim, int order, const SpeciesPtrs& sp, Fie
                                   cudaStream_t s) {
   if (sp.npart <= 0) return cudaSuccess;
   int64_t blocks = (sp.npart + 255) / 256;
-  if (blocks > 152 * 32) blocks = 152 * 32;
+  if (blocks > pic::sm_count() * 32) blocks = pic::sm_count() * 32;
   const unsigned b = (unsigned)blocks;
 #define PIC_RHO(D, O) PIC_KL(k_charge_density<D, O, real><<<b, 256, 0, s>>>(sp, rho, ng, pc, err))
   if (dim == 2) {
@@ -142,7 +142,7 @@ template <typename real>
 cudaError_t launch_particle_moments(const SpeciesPtrs& sp, double* out, cudaStream_t s) {
   if (sp.npart <= 0) return cudaSuccess;
   int64_t blocks = (sp.npart + 255) / 256;
-  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks > pic::sm_count() * 8) blocks = pic::sm_count() * 8;
   PIC_KL(k_particle_moments<real><<<(unsigned)blocks, 256, 0, s>>>(sp, out));
   return cudaGetLastError();
 }

@@ -107,15 +107,19 @@ __global__ void k_energy_total(int rows, double* scratch) {
   }
 }
 
-// device address of the scratch array on the current device; resolved once
-// per device (the host-side name of a __device__ array is not a device
-// address)
-int scratch_for_current_device(double** out) {
+// device address of the scratch array on the current device (the host-side
+// name of a __device__ array is not a device address). It is looked up again
+// on every call made outside stream capture, so a context that was destroyed
+// and recreated (cudaDeviceReset) gets the array's new address; inside a
+// capture the address of the last such call is used.
+int scratch_for_current_device(cudaStream_t s, double** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return PIC_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return PIC_ERR_UNSUPPORTED;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return PIC_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
+  if (cap == cudaStreamCaptureStatusNone || !g_scratch_ptr[dev]) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_energy_scratch) != cudaSuccess || !p) return PIC_ERR_CUDA;
     g_scratch_ptr[dev] = static_cast<double*>(p);
@@ -137,10 +141,12 @@ extern "C" int pic_field_energy_noalloc(const pic_grid* g, const void* EB, doubl
     if (g->em_stride[k] <= 0) return PIC_ERR_ARG;
   const int64_t rows = (int64_t)g->n[1] * (g->dim == 3 ? g->n[2] : 1);
   if (rows > pic::kMaxRows) return PIC_ERR_UNSUPPORTED;  // beyond the fixed scratch
-  double* scratch = nullptr;
-  int     st      = pic::scratch_for_current_device(&scratch);
-  if (st != PIC_OK) return st;
   cudaStream_t s       = (cudaStream_t)stream;
+  // an error left by the caller's earlier work is reported, not consumed
+  if (cudaPeekAtLastError() != cudaSuccess) return PIC_ERR_CUDA;
+  double* scratch = nullptr;
+  int     st      = pic::scratch_for_current_device(s, &scratch);
+  if (st != PIC_OK) return st;
   const int    threads = 256, warps = threads / 32;
   const int    blocks  = (int)((rows + warps - 1) / warps);
   if (g->real_bytes == 8) {

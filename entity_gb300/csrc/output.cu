@@ -296,7 +296,7 @@ __global__ void k_output_particles(PrtlOutArgs<real> a) {
 dim3 blocks_for(int64_t n) {
   int64_t b = (n + 255) / 256;
   if (b < 1) b = 1;
-  if (b > 152 * 32) b = 152 * 32;
+  if (b > pic::sm_count() * 32) b = pic::sm_count() * 32;
   return dim3((unsigned)b);
 }
 

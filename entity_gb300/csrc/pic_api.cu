@@ -262,6 +262,22 @@ int zero_J(pic_ctx* c, void* J, cudaStream_t s) {
 namespace pic {
 static std::atomic<long long> g_launches{ 0 };
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int sm_count() {
+  constexpr int           kMaxDevices = 64;
+  static std::atomic<int> cache[kMaxDevices];  // 0 = not yet queried
+  int                     dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (dev >= 0 && dev < kMaxDevices) {
+    const int v = cache[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v;
+  }
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+    sms = 1;
+  if (dev >= 0 && dev < kMaxDevices) cache[dev].store(sms, std::memory_order_relaxed);
+  return sms;
+}
 }  // namespace pic
 
 namespace {
@@ -776,13 +792,17 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
   const size_t  b_cnt = al(4 * (nbins + 1)), b_off = al(8 * (nbins + 1)), b_perm = al(4 * np);
   const size_t  b_ptmp = al(4 * np), b_big = al(4 * nbins), b_nbig = al(4);
   const size_t  rb     = (size_t)g.real_bytes;
-  // the arrays a sort moves, staged side by side
-  pic::GatherSet gs;
-  auto add = [&](void* arr, int esz) {
-    if (!arr) return;
-    gs.arr[gs.n] = arr;
-    gs.esz[gs.n] = esz;
-    ++gs.n;
+  // the arrays a sort moves (Particles::SortSpatially and RemoveDead,
+  // particles_sort.cpp:103-253): the state, then phi and every payload
+  // column; in batches of up to kMaxSortArrays
+  struct Moved {
+    void*   arr;
+    int     esz;
+    int64_t stride;
+  };
+  std::vector<Moved> mv;
+  auto add = [&](void* arr, int esz, int64_t stride = 1) {
+    if (arr) mv.push_back({ arr, esz, stride });
   };
   add(sp->i1, 4), add(sp->i2, 4), add(sp->dx1, 4), add(sp->dx2, 4);
   if (g.dim == 3) add(sp->i3, 4), add(sp->dx3, 4);
@@ -792,16 +812,36 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
   }
   add(sp->ux1, (int)rb), add(sp->ux2, (int)rb), add(sp->ux3, (int)rb), add(sp->weight, (int)rb);
   add(sp->tag, 2);
-  // the arrays are permuted one after the other through one staging buffer
-  const size_t b_tmp = al(np * (rb > 4 ? rb : 4));
-  const size_t  need   = b_key + b_rank + b_dead + b_drank + b_cnt + b_off + b_perm + b_ptmp + b_big +
-                      b_nbig + b_tmp;
-  if (need > c->sort_bytes) {
+  add(sp->phi, (int)rb);
+  for (int k = 0; k < sp->npld_r; ++k)
+    add((char*)sp->pld_r + (size_t)k * sp->pld_r_stride[1] * rb, (int)rb, sp->pld_r_stride[0]);
+  for (int k = 0; k < sp->npld_i; ++k)
+    add((char*)sp->pld_i + (size_t)k * sp->pld_i_stride[1] * 8, 8, sp->pld_i_stride[0]);
+  // every array of a batch gets its own staging area when the context can
+  // hold them (one gather, one copy back per batch); otherwise they go in
+  // turn through one
+  size_t b_all = 0;
+  for (size_t k = 0; k < mv.size() && k < (size_t)pic::kMaxSortArrays; ++k)
+    b_all += al((size_t)np * mv[k].esz);
+  const size_t b_big_elem = al(np * 8);
+  const size_t b_one = b_big_elem;
+  const size_t  fixed_need = b_key + b_rank + b_dead + b_drank + b_cnt + b_off + b_perm + b_ptmp +
+                            b_big + b_nbig;
+  bool          apart      = true;
+  if (fixed_need + b_all > c->sort_bytes) {
     if (c->sort_buf) cudaFree(c->sort_buf);
     c->sort_buf   = nullptr;
     c->sort_bytes = 0;
-    if (cudaMalloc(&c->sort_buf, need) != cudaSuccess) return PIC_ERR_NOMEM;
-    c->sort_bytes = need;
+    if (cudaMalloc(&c->sort_buf, fixed_need + b_all) == cudaSuccess) {
+      c->sort_bytes = fixed_need + b_all;
+    } else {
+      cudaGetLastError();  // the failed allocation leaves no sticky error
+      apart = false;
+      if (fixed_need + b_one > c->sort_bytes) {
+        if (cudaMalloc(&c->sort_buf, fixed_need + b_one) != cudaSuccess) return PIC_ERR_NOMEM;
+        c->sort_bytes = fixed_need + b_one;
+      }
+    }
   }
   char*         base = (char*)c->sort_buf;
   pic::SortArgs a;
@@ -841,12 +881,23 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
   base += b_big;
   a.nbig = (int32_t*)base;
   base += b_nbig;
-  for (int k = 0; k < gs.n; ++k) gs.tmp[k] = base;
   a.err = c->d_err;
 
   cudaError_t e = pic::sort_build_perm(a, s);
   if (e != cudaSuccess) return PIC_ERR_CUDA;
-  if ((e = pic::sort_apply_all(gs, a.perm, np, s)) != cudaSuccess) return PIC_ERR_CUDA;
+  for (size_t k0 = 0; k0 < mv.size(); k0 += pic::kMaxSortArrays) {
+    pic::GatherSet gs;
+    char*          t = base;
+    for (size_t k = k0; k < mv.size() && gs.n < pic::kMaxSortArrays; ++k) {
+      gs.arr[gs.n]    = mv[k].arr;
+      gs.esz[gs.n]    = mv[k].esz;
+      gs.stride[gs.n] = mv[k].stride;
+      gs.tmp[gs.n]    = t;
+      if (apart) t += al((size_t)np * mv[k].esz);
+      ++gs.n;
+    }
+    if ((e = pic::sort_apply_all(gs, a.perm, np, s)) != cudaSuccess) return PIC_ERR_CUDA;
+  }
   if (remove_dead) {
     // particles_sort.cpp:175-191: alive tags on the front, dead on the tail
     if ((e = pic::set_tags_after_removal(sp->tag, np, a.count + a.dead_bin, s)) != cudaSuccess)

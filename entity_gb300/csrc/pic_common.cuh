@@ -472,116 +472,6 @@ __device__ __forceinline__ bool deposit_particle(const Prtl<real>& q, real weigh
   return deposit_with_velocity<D, O, real>(q, vp, weight, charge, inv_dt, ng, ext, add);
 }
 
-// Esirkepov deposit (orders 1-3) of a particle whose initial and final
-// stencils start at the same cell along every axis: for_deposit's third case
-// (particle_shapes.hpp:1001-1015), where the (O+2)-th row of both stencils is
-// empty and the extents are O. Only the (O+1)^D box is visited, so no entry
-// carries a predicate. iS/fS are the O+1 weights of the two stencils along
-// each axis, i0 the ghost-inclusive index of their first cell. Every entry's
-// value is the expression deposit_with_velocity forms for it, so J is the same
-// as the general loop's.
-template <int D, int O, typename real, typename Add>
-__device__ __forceinline__ void deposit_same_support(const real (*iS)[O + 1],
-                                                     const real (*fS)[O + 1], const int* i0,
-                                                     real coeff, real vz, real inv_dt, Add&& add) {
-  constexpr int N    = O + 1;
-  const real    HALF = 0.5, THIRD = K<real>::THIRD;
-  const real    Q    = coeff * inv_dt;
-  if constexpr (D == 2) {
-    const real QVx3 = coeff * vz;
-    real       hd0[N], hs0[N];
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      hd0[i] = HALF * (fS[0][i] - iS[0][i]);
-      hs0[i] = HALF * (fS[0][i] + iS[0][i]);
-    }
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-      const real s1  = fS[1][j] + iS[1][j];
-      real       acc = 0;
-#pragma unroll
-      for (int i = 0; i < N - 1; ++i) {
-        const real W = hd0[i] * s1;
-        acc          = (i == 0) ? (-Q * W) : (acc - Q * W);
-        add(i0[0] + i, i0[1] + j, 0, 0, acc);
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      real acc = 0;
-#pragma unroll
-      for (int j = 0; j < N - 1; ++j) {
-        const real W = hs0[i] * (fS[1][j] - iS[1][j]);
-        acc          = (j == 0) ? (-Q * W) : (acc - Q * W);
-        add(i0[0] + i, i0[1] + j, 0, 1, acc);
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      const real ga = HALF * iS[0][i] + fS[0][i];
-      const real gb = HALF * fS[0][i] + iS[0][i];
-#pragma unroll
-      for (int j = 0; j < N; ++j) {
-        const real W = THIRD * (fS[1][j] * ga + iS[1][j] * gb);
-        add(i0[0] + i, i0[1] + j, 0, 2, QVx3 * W);
-      }
-    }
-  } else {
-    real t0[N], t1[N], t2[N];
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      t0[i] = THIRD * (fS[0][i] - iS[0][i]);
-      t1[i] = THIRD * (fS[1][i] - iS[1][i]);
-      t2[i] = THIRD * (fS[2][i] - iS[2][i]);
-    }
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-#pragma unroll
-      for (int k = 0; k < N; ++k) {
-        const real P = (iS[1][j] * iS[2][k] + fS[1][j] * fS[2][k]) +
-                       HALF * (iS[2][k] * fS[1][j] + iS[1][j] * fS[2][k]);
-        real acc = 0;
-#pragma unroll
-        for (int i = 0; i < N - 1; ++i) {
-          const real W = t0[i] * P;
-          acc          = (i == 0) ? (-Q * W) : (acc - Q * W);
-          add(i0[0] + i, i0[1] + j, i0[2] + k, 0, acc);
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-#pragma unroll
-      for (int k = 0; k < N; ++k) {
-        const real P = iS[0][i] * iS[2][k] + fS[0][i] * fS[2][k] +
-                       HALF * (iS[2][k] * fS[0][i] + iS[0][i] * fS[2][k]);
-        real acc = 0;
-#pragma unroll
-        for (int j = 0; j < N - 1; ++j) {
-          const real W = t1[j] * P;
-          acc          = (j == 0) ? (-Q * W) : (acc - Q * W);
-          add(i0[0] + i, i0[1] + j, i0[2] + k, 1, acc);
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-#pragma unroll
-      for (int j = 0; j < N; ++j) {
-        const real P = iS[0][i] * iS[1][j] + fS[0][i] * fS[1][j] +
-                       HALF * (iS[0][i] * fS[1][j] + iS[1][j] * fS[0][i]);
-        real acc = 0;
-#pragma unroll
-        for (int k = 0; k < N - 1; ++k) {
-          const real W = t2[k] * P;
-          acc          = (k == 0) ? (-Q * W) : (acc - Q * W);
-          add(i0[0] + i, i0[1] + j, i0[2] + k, 2, acc);
-        }
-      }
-    }
-  }
-}
-
 // the deposit proper, given the particle velocity vp (the GR deposit passes
 // its metric velocity, currents_deposit.hpp:138-159)
 template <int D, int O, typename real, typename Add>

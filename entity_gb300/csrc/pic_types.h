@@ -38,6 +38,10 @@ enum ErrIdx { ERR_BAD_TAG = 0, ERR_OUT_OF_GRID = 1, ERR_STENCIL_OUT = 2, ERR_SAM
 // process-wide count of kernels this library has launched
 void note_launch();
 
+// streaming multiprocessors of the current device (queried once per device;
+// 1 when the query fails); grid caps are multiples of it
+int sm_count();
+
 }  // namespace pic
 
 // launches a kernel and counts it: PIC_KL(k<<<grid, block, smem, stream>>>(args))

@@ -265,7 +265,7 @@ __global__ void k_set_tags(int16_t* tag, int64_t np, const int32_t* n_dead) {
 
 dim3 grid_n(int64_t n) {
   int64_t b = (n + 255) / 256;
-  if (b > 152 * 64) b = 152 * 64;
+  if (b > pic::sm_count() * 64) b = pic::sm_count() * 64;
   if (b < 1) b = 1;
   return dim3((unsigned)b);
 }
@@ -296,16 +296,143 @@ cudaError_t sort_build_perm(SortArgs a, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     PIC_KL(k_fix_small<<<grid_n(a.dead_bin), 256, 0, s>>>(a));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    PIC_KL(k_fix_big<<<152 * 2, 256, 0, s>>>(a));
+    PIC_KL(k_fix_big<<<pic::sm_count() * 2, 256, 0, s>>>(a));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
+namespace {
+// arr_k[i] -> dst_k[i] = arr_k[perm[i]] for every listed array: the
+// permutation is read once per particle for all arrays of the species
+struct MultiGather {
+  const void* src[kMaxSortArrays];
+  void*       dst[kMaxSortArrays];
+  int         esz[kMaxSortArrays];
+  int64_t     es[kMaxSortArrays];  // element stride of src
+  int         n;
+};
+
+__global__ void k_gather_multi(MultiGather g, const int32_t* __restrict__ perm, int64_t np) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np; i += stride) {
+    const int64_t j = perm[i];
+    for (int k = 0; k < g.n; ++k) {
+      const int64_t jk = j * g.es[k];
+      if (g.esz[k] == 4)
+        ((int32_t*)g.dst[k])[i] = ((const int32_t*)g.src[k])[jk];
+      else if (g.esz[k] == 8)
+        ((int64_t*)g.dst[k])[i] = ((const int64_t*)g.src[k])[jk];
+      else
+        ((int16_t*)g.dst[k])[i] = ((const int16_t*)g.src[k])[jk];
+    }
+  }
+}
+
+// copies of the packed staging areas back into the caller's arrays: packed
+// arrays in 16-byte pieces where both ends allow it (chunk c of array k
+// covers bytes [c * 16, c * 16 + 16)), strided ones element by element
+// (chunk c is element c)
+struct MultiCopy {
+  const char* src[kMaxSortArrays];
+  char*       dst[kMaxSortArrays];
+  int64_t     bytes[kMaxSortArrays];
+  int64_t     es[kMaxSortArrays];  // element stride of dst
+  int         esz[kMaxSortArrays];
+  int64_t     first_chunk[kMaxSortArrays + 1];
+  int         vec[kMaxSortArrays];  // packed, both pointers 16-byte aligned
+  int         n;
+};
+
+__global__ void k_copy_multi(MultiCopy m) {
+  const int64_t total  = m.first_chunk[m.n];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int           k      = 0;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total; c += stride) {
+    while (c >= m.first_chunk[k + 1]) ++k;
+    const int64_t q = c - m.first_chunk[k];
+    if (m.es[k] != 1) {
+      const int64_t d = q * m.es[k];
+      if (m.esz[k] == 4)      ((int32_t*)m.dst[k])[d] = ((const int32_t*)m.src[k])[q];
+      else if (m.esz[k] == 8) ((int64_t*)m.dst[k])[d] = ((const int64_t*)m.src[k])[q];
+      else                    ((int16_t*)m.dst[k])[d] = ((const int16_t*)m.src[k])[q];
+      continue;
+    }
+    const int64_t off = q * 16;
+    const int64_t len = m.bytes[k] - off < 16 ? m.bytes[k] - off : 16;
+    if (m.vec[k] && len == 16) {
+      *(int4*)(m.dst[k] + off) = *(const int4*)(m.src[k] + off);
+    } else {
+      for (int64_t b = 0; b < len; ++b) m.dst[k][off + b] = m.src[k][off + b];
+    }
+  }
+}
+
+// one array through a shared staging buffer, any element stride
+template <typename T>
+__global__ void k_gather_strided(const T* __restrict__ src, T* __restrict__ dst,
+                                 const int32_t* perm, int64_t n, int64_t es) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    dst[i] = src[(int64_t)perm[i] * es];
+}
+template <typename T>
+__global__ void k_unpack_strided(const T* __restrict__ src, T* __restrict__ dst, int64_t n,
+                                 int64_t es) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    dst[i * es] = src[i];
+}
+}  // namespace
+
 cudaError_t sort_apply_all(const GatherSet& g, const int32_t* perm, int64_t n, cudaStream_t s) {
   if (n <= 0 || g.n == 0) return cudaSuccess;
   cudaError_t e = cudaSuccess;
+  bool        staged_apart = true;  // every array has its own staging area
+  for (int k = 0; k < g.n && staged_apart; ++k)
+    for (int q = 0; q < k; ++q) staged_apart = staged_apart && g.tmp[q] != g.tmp[k];
+  if (staged_apart) {
+    // one gather of all arrays (perm read once), then one copy back
+    MultiGather mg{};
+    MultiCopy   mc{};
+    mg.n = mc.n = g.n;
+    mc.first_chunk[0] = 0;
+    for (int k = 0; k < g.n; ++k) {
+      mg.src[k] = g.arr[k];
+      mg.dst[k] = g.tmp[k];
+      mg.esz[k] = g.esz[k];
+      mg.es[k]  = g.stride[k];
+      mc.src[k] = (const char*)g.tmp[k];
+      mc.dst[k] = (char*)g.arr[k];
+      mc.bytes[k] = n * g.esz[k];
+      mc.es[k]    = g.stride[k];
+      mc.esz[k]   = g.esz[k];
+      mc.vec[k] = g.stride[k] == 1 && ((uintptr_t)g.tmp[k] % 16 == 0) &&
+                  ((uintptr_t)g.arr[k] % 16 == 0);
+      mc.first_chunk[k + 1] =
+        mc.first_chunk[k] + (g.stride[k] == 1 ? (mc.bytes[k] + 15) / 16 : n);
+    }
+    PIC_KL(k_gather_multi<<<grid_n(n), 256, 0, s>>>(mg, perm, n));
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    PIC_KL(k_copy_multi<<<grid_n(mc.first_chunk[g.n]), 256, 0, s>>>(mc));
+    return cudaGetLastError();
+  }
+  // one shared staging buffer: the arrays go in turn
   for (int k = 0; k < g.n; ++k) {
+    if (g.stride[k] != 1) {
+      if (g.esz[k] == 8) {
+        PIC_KL(k_gather_strided<int64_t><<<grid_n(n), 256, 0, s>>>((const int64_t*)g.arr[k], (int64_t*)g.tmp[k], perm, n, g.stride[k]));
+        PIC_KL(k_unpack_strided<int64_t><<<grid_n(n), 256, 0, s>>>((const int64_t*)g.tmp[k], (int64_t*)g.arr[k], n, g.stride[k]));
+      } else if (g.esz[k] == 4) {
+        PIC_KL(k_gather_strided<int32_t><<<grid_n(n), 256, 0, s>>>((const int32_t*)g.arr[k], (int32_t*)g.tmp[k], perm, n, g.stride[k]));
+        PIC_KL(k_unpack_strided<int32_t><<<grid_n(n), 256, 0, s>>>((const int32_t*)g.tmp[k], (int32_t*)g.arr[k], n, g.stride[k]));
+      } else {
+        PIC_KL(k_gather_strided<int16_t><<<grid_n(n), 256, 0, s>>>((const int16_t*)g.arr[k], (int16_t*)g.tmp[k], perm, n, g.stride[k]));
+        PIC_KL(k_unpack_strided<int16_t><<<grid_n(n), 256, 0, s>>>((const int16_t*)g.tmp[k], (int16_t*)g.arr[k], n, g.stride[k]));
+      }
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      continue;
+    }
     if (g.esz[k] == 4)
       PIC_KL(k_gather<int32_t><<<grid_n(n), 256, 0, s>>>((const int32_t*)g.arr[k], (int32_t*)g.tmp[k], perm, n));
     else if (g.esz[k] == 8)

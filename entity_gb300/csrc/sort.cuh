@@ -64,13 +64,16 @@ struct SortArgs {
 cudaError_t sort_build_perm(SortArgs a, cudaStream_t s);
 
 // every listed array permuted in place: arr_k[i] <- arr_k[perm[i]], staged
-// through tmp_k (the tmp_k may share one buffer: the arrays go in turn)
-constexpr int kMaxSortArrays = 20;  // 3D with prev arrays needs 17
+// through tmp_k. With a staging area per array, one kernel gathers all
+// arrays (the permutation read once) and one copies them back; when the
+// tmp_k share one buffer the arrays go in turn
+constexpr int kMaxSortArrays = 32;  // 3D with prev arrays needs 17, phi and payloads more
 struct GatherSet {
-  void* arr[kMaxSortArrays];
-  void* tmp[kMaxSortArrays];
-  int   esz[kMaxSortArrays];  // element bytes: 2, 4 or 8
-  int   n = 0;
+  void*   arr[kMaxSortArrays];
+  void*   tmp[kMaxSortArrays];
+  int     esz[kMaxSortArrays];     // element bytes: 2, 4 or 8
+  int64_t stride[kMaxSortArrays];  // element stride of arr (payload columns); tmp is packed
+  int     n = 0;
 };
 cudaError_t sort_apply_all(const GatherSet& g, const int32_t* perm, int64_t n, cudaStream_t s);
 

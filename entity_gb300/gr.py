@@ -112,6 +112,10 @@ class GRContext(Context):
     def gr_average(self, which, a, b, stream=None):
         abi.call("pic_gr_average", self.h, which, _ptr(a), _ptr(b), _stream_ptr(stream))
 
+    def gr_filter_currents(self, J, buff, npasses, stream=None):
+        abi.call("pic_gr_filter_currents", self.h, C.byref(self.m), _ptr(J), _ptr(buff),
+                 int(npasses), _stream_ptr(stream))
+
     def gr_field_bcs(self, fld, set_e, set_b, nfilter=0, stream=None):
         abi.call("pic_gr_field_bcs", self.h, C.byref(self.m), _ptr(fld), int(set_e), int(set_b),
                  nfilter, _stream_ptr(stream))

@@ -2,8 +2,8 @@
 // ABI: the leapfrog of D, B (em at the newer time, em0 at the older one),
 // the auxiliary E and H, the GR push and deposit, and the field swap, with
 // the axis, horizon and (optionally) MATCH field boundaries and the current
-// absorption at r max. CommunicateFields and SynchronizeFields are no-ops on
-// one non-periodic (r, theta) domain; the current filter is not applied.
+// absorption at r max, and the current filter. CommunicateFields and
+// SynchronizeFields are no-ops on one non-periodic (r, theta) domain.
 #include <cstdint>
 #include <cuda_runtime.h>
 #include <utility>
@@ -101,6 +101,8 @@ int gr_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species* sp, int32_t nsp, 
                            stream));
     // FieldBoundaries(gr_bc::curr): absorbing particles at r max (fields_bcs.h:262-268)
     if (match && absorb_max) PIC_TRY(pic_gr_absorb_currents(ctx, m, f[4], gp.match_ds, stream));
+    // CurrentsFilter on cur0 (grpic.hpp:437-439)
+    if (p.nfilter > 0) PIC_TRY(pic_gr_filter_currents(ctx, m, f[4], f[5], p.nfilter, stream));
   }
   PIC_TRY(mark(PIC_PHASE_PUSH_DEPOSIT, 1));
   if (fs) {
@@ -141,7 +143,8 @@ extern "C" int pic_grpic_step(pic_ctx* ctx, const pic_gr_metric* m, pic_species*
     return PIC_ERR_ARG;
   for (int k = 0; k < 5; ++k)
     if (!fields[k]) return PIC_ERR_ARG;
-  if (prm->nfilter != 0 || gprm->niter < 1) return PIC_ERR_UNSUPPORTED;
+  if (prm->nfilter < 0 || (prm->nfilter > 0 && !fields[5])) return PIC_ERR_ARG;
+  if (gprm->niter < 1) return PIC_ERR_UNSUPPORTED;
   if (gprm->match_ds < 0.0 || (gprm->match_ds > 0.0 && !gprm->match_target)) return PIC_ERR_ARG;
   pic_grid g;
   int      st = pic_get_grid(ctx, &g);

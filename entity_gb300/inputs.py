@@ -81,26 +81,39 @@ class SpeciesArrays:
     pusher: int = 1
     npart: int = 0
     index: int = 1
+    # optional: phi (real, 1D) and the payloads, 2D (particles x columns)
+    # tensors of real (pld_r) and int64 (pld_i) with any strides
+    phi: torch.Tensor = None
+    pld_r: torch.Tensor = None
+    pld_i: torch.Tensor = None
+
+    def _extras(self, f):
+        return [None if x is None else f(x) for x in (self.phi, self.pld_r, self.pld_i)]
 
     def to(self, device):
         mv = lambda xs: [None if x is None else x.to(device) for x in xs]
         return SpeciesArrays(mv(self.i), mv(self.dx), mv(self.i_prev), mv(self.dx_prev),
                              mv(self.u), self.w.to(device), self.tag.to(device), self.mass,
-                             self.charge, self.pusher, self.npart, self.index)
+                             self.charge, self.pusher, self.npart, self.index,
+                             *self._extras(lambda x: x.to(device)))
 
     def astype(self, real):
         """A copy whose momenta and weights are converted to `real` (cells,
         offsets and tags are shared as copies)."""
         cl = lambda xs: [None if x is None else x.clone() for x in xs]
+        phi, pr, pi = self._extras(lambda x: x.clone())
         return SpeciesArrays(cl(self.i), cl(self.dx), cl(self.i_prev), cl(self.dx_prev),
                              [x.to(real) for x in self.u], self.w.to(real), self.tag.clone(),
-                             self.mass, self.charge, self.pusher, self.npart, self.index)
+                             self.mass, self.charge, self.pusher, self.npart, self.index,
+                             None if phi is None else phi.to(real),
+                             None if pr is None else pr.to(real), pi)
 
     def clone(self):
         cl = lambda xs: [None if x is None else x.clone() for x in xs]
         return SpeciesArrays(cl(self.i), cl(self.dx), cl(self.i_prev), cl(self.dx_prev),
                              cl(self.u), self.w.clone(), self.tag.clone(), self.mass,
-                             self.charge, self.pusher, self.npart, self.index)
+                             self.charge, self.pusher, self.npart, self.index,
+                             *self._extras(lambda x: x.clone(memory_format=torch.preserve_format)))
 
 
 def empty_species(g: GridSpec, capacity: int, *, mass=1.0, charge=-1.0, pusher=1, index=1,

@@ -82,6 +82,15 @@ def make_species(sp: SpeciesArrays, dim: int) -> abi.PicSpecies:
     ps.charge = sp.charge
     ps.pusher = sp.pusher
     ps.index = sp.index
+    if getattr(sp, "phi", None) is not None:
+        ps.phi = _ptr(sp.phi)
+    for name in ("pld_r", "pld_i"):
+        t = getattr(sp, name, None)
+        if t is not None and t.numel() > 0:
+            setattr(ps, name, _ptr(t))
+            st = getattr(ps, name + "_stride")
+            st[0], st[1] = t.stride(0), t.stride(1)
+            setattr(ps, "n" + name, t.shape[1])
     return ps
 
 

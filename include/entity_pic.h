@@ -97,7 +97,13 @@ typedef struct {
 /* One species as structure of arrays, field for field the reference's
  * ParticleArrays (src/framework/containers/particles.h:47-71). ux*, weight are
  * real_t; i*_prev / dx*_prev may be NULL when PIC_PD_WRITE_PREV is not set
- * and the sort is asked to skip them. i3-arrays are unused in 2D. */
+ * and the sort is asked to skip them. i3-arrays are unused in 2D.
+ * The trailing fields are optional (zero them when unused): phi (real_t, the
+ * reference keeps it for 2D non-Cartesian grids) and the payloads pld_r
+ * (real_t) and pld_i (npart_t, 64-bit), npld_r / npld_i columns each, element
+ * (p, k) at pld[p * pld_stride[0] + k * pld_stride[1]] (elements; a Kokkos
+ * LayoutLeft View on the device has strides {1, maxnpart}). Only the sort and
+ * dead removal touch them: particles carry their phi and payloads along. */
 typedef struct {
   int32_t *i1, *i2, *i3;
   int32_t *i1_prev, *i2_prev, *i3_prev;
@@ -112,6 +118,13 @@ typedef struct {
   float    charge;
   int32_t  pusher; /* PIC_PUSHER_* */
   int32_t  index;  /* species index (1-based as in the reference) */
+  void*    phi;
+  void*    pld_r;
+  void*    pld_i;
+  int64_t  pld_r_stride[2];
+  int64_t  pld_i_stride[2];
+  int32_t  npld_r;
+  int32_t  npld_i;
 } pic_species;
 
 typedef struct pic_ctx pic_ctx;
@@ -245,10 +258,12 @@ int pic_field_energy(pic_ctx* ctx, const void* EB, double dx, double* out, void*
  * scratch is a fixed 1 MiB array inside the library, one slot pair per grid
  * row, so grids with more than 65536 rows (n2 * n3 in 3D, n2 in 2D) are
  * rejected with PIC_ERR_UNSUPPORTED. The first call on a device resolves the
- * array's device address, so make it before any stream capture. Calls share
- * the array: calls that overlap on the GPU race and must be serialised. The
- * result is computed in a fixed order (bitwise reproducible). Synchronises
- * the stream. */
+ * array's device address, so make it before any stream capture; later calls
+ * outside capture look it up again (a reset device gets the new address).
+ * Calls share the array: calls that overlap on the GPU race and must be
+ * serialised. An error already pending from the caller's earlier work is
+ * returned as PIC_ERR_CUDA without being cleared. The result is computed in a
+ * fixed order (bitwise reproducible). Synchronises the stream. */
 int pic_field_energy_noalloc(const pic_grid* grid, const void* EB, double dx, double* out,
                              void* stream);
 
@@ -514,6 +529,14 @@ int pic_gr_aux(pic_ctx* ctx, const pic_gr_metric* m, int32_t which, const void* 
  * TimeAverageJ (which = 1: a = (b + a) / 2 over the 3 current components),
  * active cells (aux_fields_gr.hpp:214-280) */
 int pic_gr_average(pic_ctx* ctx, int32_t which, void* a, void* b, void* stream);
+/* grpic::CurrentsFilter (src/engines/grpic/currents.h:74-101): npasses times
+ * buff <- J, then DigitalFilter_kernel's 2D non-Cartesian stencil
+ * (src/kernels/digital_filter.hpp:196-276) from buff into J over the active
+ * cells and the row above them, with the reference's one-sided theta weights
+ * on the rows next to an axis (m's axis flags). The exchange that follows
+ * each pass in the reference is a no-op on one non-periodic domain. */
+int pic_gr_filter_currents(pic_ctx* ctx, const pic_gr_metric* m, void* J, void* buff,
+                           int32_t npasses, void* stream);
 /* AxisBoundaries_kernel and HorizonBoundaries_kernel (fields_bcs.hpp:825-868,
  * 1188-1240) on one field, per m's axis/horizon flags; set_e / set_b select
  * the D (E) and B (H) components */
@@ -553,7 +576,8 @@ typedef struct {
  * domain: fields[0..5] = em, em0, aux, cur, cur0, buff (device pointers);
  * the step swaps em <-> em0 and cur <-> cur0 in the array as the reference
  * swaps its views. Step 0 runs the reference's initialisation block.
- * Filters are not supported (nfilter must be 0). With gprm->match_ds > 0
+ * prm->nfilter passes of pic_gr_filter_currents follow the deposit and the
+ * current absorption (fields[5] is the filter's buffer). With gprm->match_ds > 0
  * the MATCH boundary at r max follows the axis and horizon boundaries on em
  * and em0 (FieldBoundaries, gr_bc::main), and, when particles are absorbed
  * at r max, the currents are absorbed there after the deposit (gr_bc::curr). */

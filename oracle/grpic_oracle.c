@@ -488,6 +488,76 @@ void orc_gr_average_j(const orc_grid* g, void* J_, const void* J0_) {
         J[JI(g, i1, i2, c)] = (real)0.5 * (J0[JI(g, i1, i2, c)] + J[JI(g, i1, i2, c)]);
 }
 
+void orc_gr_filter_pass(const orc_grid* g, void* J_, void* buff_, int axis_min, int axis_max) {
+  /* grpic::CurrentsFilter (src/engines/grpic/currents.h:74-101), one pass:
+   * buff <- cur0 (the whole array), then DigitalFilter_kernel's 2D
+   * non-Cartesian branch (src/kernels/digital_filter.hpp:196-276) over
+   * i1 in [i1min, i1max), i2 in [i2min, i2max] with the axis rows */
+  /* src/global/utils/numeric.h: ZERO, INV_2, INV_4, INV_8, INV_16 */
+  const real  ZERO = 0, INV_2 = 0.5, INV_4 = 0.25, INV_8 = 0.125, INV_16 = 0.0625;
+  real*       J  = (real*)J_;
+  real*       B  = (real*)buff_;
+  const int   ng = g->ng;
+  const int   N1 = g->n1 + 2 * ng, N2 = g->n2 + 2 * ng;
+  for (int i2 = 0; i2 < N2; ++i2)
+    for (int i1 = 0; i1 < N1; ++i1)
+      for (int c = 0; c < 3; ++c) B[JI(g, i1, i2, c)] = J[JI(g, i1, i2, c)];
+  const int   i2min = ng, i2max = g->n2 + ng;
+#define F1(c, a, b) (INV_2 * B[JI(g, a, b, c)] + INV_4 * (B[JI(g, (a) - 1, b, c)] + B[JI(g, (a) + 1, b, c)]))
+  for (int i2 = i2min; i2 <= i2max; ++i2) {
+    for (int i1 = ng; i1 < g->n1 + ng; ++i1) {
+      real c00, c0p1, c0m1;
+      if (axis_min && i2 == i2min) {
+        c00  = F1(0, i1, i2);
+        c0p1 = F1(0, i1, i2 + 1);
+        J[JI(g, i1, i2, 0)] = INV_2 * c00 + INV_2 * c0p1;
+        J[JI(g, i1, i2, 2)] = ZERO;
+        c00  = F1(1, i1, i2);
+        c0p1 = F1(1, i1, i2 + 1);
+        J[JI(g, i1, i2, 1)] = INV_4 * (c00 + c0p1);
+      } else if (axis_min && i2 == i2min + 1) {
+        c00  = F1(0, i1, i2);
+        c0p1 = F1(0, i1, i2 + 1);
+        c0m1 = F1(0, i1, i2 - 1);
+        J[JI(g, i1, i2, 0)] = INV_2 * c00 + INV_4 * (c0p1 + c0m1);
+        c00  = F1(2, i1, i2);
+        c0p1 = F1(2, i1, i2 + 1);
+        J[JI(g, i1, i2, 2)] = INV_2 * c00 + INV_4 * c0p1;
+        c00  = F1(1, i1, i2);
+        c0p1 = F1(1, i1, i2 + 1);
+        c0m1 = F1(1, i1, i2 - 1);
+        J[JI(g, i1, i2, 1)] = INV_2 * c00 + INV_4 * (c0m1 + c0p1);
+      } else if (axis_max && i2 == i2max - 1) {
+        c00  = F1(0, i1, i2);
+        c0p1 = F1(0, i1, i2 + 1);
+        c0m1 = F1(0, i1, i2 - 1);
+        J[JI(g, i1, i2, 0)] = INV_2 * c00 + INV_4 * (c0m1 + c0p1);
+        c00  = F1(2, i1, i2);
+        c0m1 = F1(2, i1, i2 - 1);
+        J[JI(g, i1, i2, 2)] = INV_2 * c00 + INV_4 * c0m1;
+        c00  = F1(1, i1, i2);
+        c0m1 = F1(1, i1, i2 - 1);
+        J[JI(g, i1, i2, 1)] = INV_4 * (c00 + c0m1);
+      } else if (axis_max && i2 == i2max) {
+        c00  = F1(0, i1, i2);
+        c0m1 = F1(0, i1, i2 - 1);
+        J[JI(g, i1, i2, 0)] = INV_2 * c00 + INV_2 * c0m1;
+        J[JI(g, i1, i2, 2)] = ZERO;
+      } else {
+        for (int c = 0; c < 3; ++c) {
+          J[JI(g, i1, i2, c)] =
+            INV_4 * B[JI(g, i1, i2, c)] +
+            INV_8 * (B[JI(g, i1 - 1, i2, c)] + B[JI(g, i1 + 1, i2, c)] +
+                     B[JI(g, i1, i2 - 1, c)] + B[JI(g, i1, i2 + 1, c)]) +
+            INV_16 * (B[JI(g, i1 - 1, i2 - 1, c)] + B[JI(g, i1 + 1, i2 + 1, c)] +
+                      B[JI(g, i1 - 1, i2 + 1, c)] + B[JI(g, i1 + 1, i2 - 1, c)]);
+        }
+      }
+    }
+  }
+#undef F1
+}
+
 void orc_gr_field_bcs(const orc_grid* g, void* fld_, int set_e, int set_b, int axis_min,
                       int axis_max, int horizon, int nfilter) {
   real*     F  = (real*)fld_;

@@ -85,6 +85,9 @@ void orc_gr_aux_h(const orc_grid* g, const orc_qks* q, const void* D, const void
  * (J = (J0 + J) / 2), active cells */
 void orc_gr_average_db(const orc_grid* g, const void* f, void* f0);
 void orc_gr_average_j(const orc_grid* g, void* J, const void* J0);
+/* one pass of grpic::CurrentsFilter: buff <- J, then the 2D axisymmetric
+ * stencil of DigitalFilter_kernel with the axis rows (axis_min / axis_max) */
+void orc_gr_filter_pass(const orc_grid* g, void* J, void* buff, int axis_min, int axis_max);
 /* AxisBoundaries_kernel and HorizonBoundaries_kernel on one field: set_e /
  * set_b select the components (D/E and B/H) */
 void orc_gr_field_bcs(const orc_grid* g, void* fld, int set_e, int set_b, int axis_min,

@@ -383,6 +383,7 @@ def _gr_sigs(L):
     L.orc_gr_aux_h.argtypes = [G, Q, V, V, V, C.c_int]
     L.orc_gr_average_db.argtypes = [G, V, V]
     L.orc_gr_average_j.argtypes = [G, V, V]
+    L.orc_gr_filter_pass.argtypes = [G, V, V, C.c_int, C.c_int]
     L.orc_gr_field_bcs.argtypes = [G, V, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
     L.orc_gr_match.argtypes = [G, Q, V, V, D, D, D, C.c_int, C.c_int, C.c_int, C.c_int]
     L.orc_gr_absorb_currents.argtypes = [G, Q, V, D, D, D]
@@ -473,6 +474,9 @@ class GROracle(Oracle):
     def gr_average_j(self, J, J0):
         self.L.orc_gr_average_j(C.byref(self.og), _p(J), _p(J0))
 
+    def gr_filter_pass(self, J, buff, axis_min=1, axis_max=1):
+        self.L.orc_gr_filter_pass(C.byref(self.og), _p(J), _p(buff), axis_min, axis_max)
+
     def gr_field_bcs(self, fld, set_e, set_b, axis_min=1, axis_max=1, horizon=1, nfilter=0):
         self.L.orc_gr_field_bcs(C.byref(self.og), _p(fld), int(set_e), int(set_b), axis_min,
                                 axis_max, horizon, nfilter)
@@ -540,6 +544,8 @@ class GROracle(Oracle):
             self.gr_deposit(species, fields[4], float(dt), island=island)
             if match is not None and self.g.prtl_bc[0][1] == 1:
                 self.gr_absorb_currents(fields[4], match[0])
+            for _ in range(prm.nfilter):
+                self.gr_filter_pass(fields[4], fields[5], amin, amax)
         if fs:
             cur, cur0 = fields[3], fields[4]
             if dep:

@@ -46,6 +46,8 @@ def lib(real, order):
         L.ref_currents_ampere.argtypes = [G, V, V, D, D]
         L.ref_filter_pass.restype = C.c_int
         L.ref_filter_pass.argtypes = [G, V, V]
+        L.ref_filter_pass_axisym.restype = C.c_int
+        L.ref_filter_pass_axisym.argtypes = [G, V, V, C.c_int, C.c_int]
         L.ref_sort_keys.restype = C.c_int
         L.ref_sort_keys.argtypes = [G, S, C.POINTER(C.c_uint32)]
         _libs[key] = L
@@ -89,6 +91,10 @@ class RefOracle(Oracle):
 
     def filter_pass(self, J, buff):
         _check(self.R.ref_filter_pass(C.byref(self.og), _p(J), _p(buff)))
+
+    def gr_filter_pass(self, J, buff, axis_min=1, axis_max=1):
+        _check(self.R.ref_filter_pass_axisym(C.byref(self.og), _p(J), _p(buff), axis_min,
+                                             axis_max))
 
     def sort_keys(self, sp):
         s = self.species(sp)

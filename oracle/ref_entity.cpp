@@ -255,6 +255,24 @@ namespace {
                          kernel::DigitalFilter_kernel<D, Coord::Cartesian>(cur, buf, size, bcs));
   }
 
+  // one pass of grpic::CurrentsFilter (src/engines/grpic/currents.h:74-101)
+  // on a 2D non-Cartesian grid: the range runs one row past the last active
+  // row (the upper axis row); the radial sides are not filtered specially
+  void filter_pass_axisym(const orc_grid* g, void* J, void* buff, int axis_min, int axis_max) {
+    auto cur = wrap_field<Dim::_2D, 3>(g, J, g->cur_s);
+    auto buf = wrap_field<Dim::_2D, 3>(g, buff, g->cur_s);
+    ncells_t size[2] = { (ncells_t)g->n1, (ncells_t)g->n2 };
+    boundaries_t<FldsBC> bcs = { { FldsBC::HORIZON, FldsBC::MATCH },
+                                 { axis_min ? FldsBC::AXIS : FldsBC::FIXED,
+                                   axis_max ? FldsBC::AXIS : FldsBC::FIXED } };
+    Kokkos::deep_copy(buf, cur);
+    Kokkos::parallel_for(
+      "CurrentsFilter",
+      range_t<Dim::_2D>({ N_GHOSTS, N_GHOSTS },
+                        { N_GHOSTS + (ncells_t)g->n1, N_GHOSTS + (ncells_t)g->n2 + 1 }),
+      kernel::DigitalFilter_kernel<Dim::_2D, Coord::Qspherical>(cur, buf, size, bcs));
+  }
+
   // sort::PositionToTileIndex<D, false> with tile size 1 (the key of
   // Particles::SortSpatially, src/framework/containers/particles_sort.cpp:196-253)
   template <Dimension D>
@@ -345,6 +363,14 @@ int ref_filter_pass(const orc_grid* g, void* J, void* buff) {
     g,
     [&] { filter_pass<Dim::_2D>(g, J, buff); },
     [&] { filter_pass<Dim::_3D>(g, J, buff); });
+}
+
+int ref_filter_pass_axisym(const orc_grid* g, void* J, void* buff, int axis_min, int axis_max) {
+  if (g->ng != (int)N_GHOSTS || g->dim != 2) {
+    return -1;
+  }
+  filter_pass_axisym(g, J, buff, axis_min, axis_max);
+  return 0;
 }
 
 int ref_sort_keys(const orc_grid* g, const orc_species* sp, std::uint32_t* keys) {

@@ -272,6 +272,58 @@ def test_grpic_step_matches_oracle(real):
 
 
 @pytest.mark.parametrize("real", REALS)
+def test_gr_current_filter_matches_oracle(real):
+    # grpic::CurrentsFilter's axisymmetric stencil with the axis rows: pure
+    # arithmetic in the reference's order, so bit-exact over three passes
+    from entity_gb300.inputs import empty_field
+    from tests.helpers import random_currents
+    g, spec, ctx, o = _setup(real, order=2)
+    J = random_currents(g, 23)
+    Jg = J.cuda()
+    for _ in range(3):
+        o.gr_filter_pass(J, empty_field(g, 3))
+    ctx.gr_filter_currents(Jg, empty_field(g, 3, "cuda"), 3)
+    torch.cuda.synchronize()
+    assert torch.equal(J, Jg.cpu())
+
+
+@pytest.mark.parametrize("real", REALS)
+def test_grpic_step_with_filter_matches_oracle(real):
+    """Five GR steps with two current-filter passes per step (nfilter = 2,
+    the horizon boundary's source row shifted accordingly)."""
+    from entity_gb300.gr import gr_step_params, horizon_island, inject_pairs
+    from entity_gb300.inputs import empty_field
+    g, spec, ctx, o = _setup(real, order=2, n=(64, 48), r_max=15.0)
+    em = empty_field(g, 6, "cuda")
+    ctx.gr_init_vertical(em)
+    fields = [em, torch.zeros_like(em), torch.zeros_like(em), empty_field(g, 3, "cuda"),
+              empty_field(g, 3, "cuda"), empty_field(g, 3, "cuda")]
+    species = inject_pairs(g, spec, 2, 5.0, 3)
+    prm = gr_step_params(ctx, cfl=0.5, ppc0=2.0, skindepth0=0.5, larmor0=0.25)
+    prm.nfilter = 2
+    island = horizon_island(g, spec)
+    cpu_fields = [f.cpu().clone() for f in fields]
+    cpu_species = [s.clone().to("cpu") for s in species]
+    for step in range(5):
+        ctx.grpic_step(species, fields, prm, niter=10, island=island, step=step)
+        o.grpic_step(cpu_species, cpu_fields, prm, niter=10, island=island, step=step)
+    torch.cuda.synchronize()
+    assert ctx.device_errors() == [0, 0, 0, 0]
+    tol = 2e-3 if real == torch.float32 else 1e-9
+    for k, name in ((0, "em"), (1, "em0"), (3, "cur"), (4, "cur0")):
+        a, b = cpu_fields[k].double(), fields[k].cpu().double()
+        for c in range(a.shape[0]):
+            scale = float(a[c].abs().max())
+            if scale == 0:
+                continue
+            err = float((a[c] - b[c]).abs().max()) / scale
+            assert err <= tol, (name, c, err)
+    for so, sg in zip(cpu_species, species):
+        assert so.npart == sg.npart
+        assert torch.equal(so.tag, sg.tag.cpu())
+
+
+@pytest.mark.parametrize("real", REALS)
 def test_gr_magnetic_flux_stays_divergence_free(real):
     """The vertical seed field comes from a vector potential, so its discrete
     divergence d_r(sqrt h B^r) + d_theta(sqrt h B^theta) vanishes; the GR

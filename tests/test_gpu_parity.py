@@ -287,6 +287,56 @@ def test_sort_bitexact(dim, flags):
     assert torch.equal(sp.w, spg.w.cpu())
 
 
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("flags", [abi.PIC_SORT_SPATIAL,
+                                   abi.PIC_SORT_SPATIAL | abi.PIC_SORT_REMOVE_DEAD,
+                                   abi.PIC_SORT_SPATIAL | abi.PIC_SORT_TILED])
+def test_sort_carries_phi_and_payloads(flags, real):
+    # Particles::SortSpatially and RemoveDead move phi and every payload column
+    # with the particle (particles_sort.cpp:169-177, 245-251): payloads in the
+    # reference's device layout (column-major, pld(p, k) at p + k * maxnpart)
+    # for the real ones and row-major for the integer ones; pld_i[:, 0] holds
+    # each particle's original index
+    g = _grid(3, 2, real)
+    sp = make_species(g, 5, 0.2, 0.0, 44)
+    n = sp.npart
+    gen = torch.Generator()
+    gen.manual_seed(9)
+    sp.tag[torch.rand(n, generator=gen) < 0.1] = 0
+    sp.phi = torch.rand(n, generator=gen, dtype=torch.float64).to(real)
+    sp.pld_r = torch.rand(3, n, generator=gen, dtype=torch.float64).to(real).t()  # strides (1, n)
+    sp.pld_i = torch.stack([torch.arange(n, dtype=torch.int64),
+                            torch.randint(0, 1 << 40, (n,), generator=gen)], dim=1)
+    assert sp.pld_r.stride() == (1, n) and sp.pld_i.stride() == (2, 1)
+    ref = sp.clone()
+    spg = sp.clone().to("cuda")
+    assert spg.pld_r.stride() == (1, n)
+    ctx = Context(g)
+    assert ctx.sort(spg, flags) == abi.PIC_OK
+    torch.cuda.synchronize()
+    m = spg.npart
+    orig = spg.pld_i[:m, 0].cpu()
+    # a permutation of the original particles (the alive ones after removal)
+    assert torch.equal(orig.sort().values,
+                       (torch.nonzero(ref.tag == 1).flatten() if flags & abi.PIC_SORT_REMOVE_DEAD
+                        else torch.arange(n)))
+    for d in range(3):
+        assert torch.equal(spg.i[d][:m].cpu(), ref.i[d][orig])
+        assert torch.equal(spg.u[d][:m].cpu(), ref.u[d][orig])
+    assert torch.equal(spg.phi[:m].cpu(), ref.phi[orig])
+    assert torch.equal(spg.pld_r[:m].cpu(), ref.pld_r[orig])
+    assert torch.equal(spg.pld_i[:m].cpu(), ref.pld_i[orig])
+    # and the order is the oracle's
+    o = _oracle(g)
+    if flags & abi.PIC_SORT_REMOVE_DEAD:
+        o.remove_dead(sp)
+    if flags & abi.PIC_SORT_TILED:
+        o.sort_tiled(sp, ctx.tile_shape())
+    else:
+        o.sort(sp)
+    _assert_particles_equal(sp, spg, 3)
+
+
 def test_sort_large_cells_and_many_dead():
     # bins over 32 entries take the block-per-bin path; the dead bin is large
     g = GridSpec(dim=2, n=(4, 4, 1), order=1, real=torch.float32)

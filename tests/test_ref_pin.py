@@ -310,3 +310,21 @@ def test_step_scales_match_reference(case, real):
     assert prm.correction == corr
     assert prm.ppc0 == ppc0
     assert prm.dx == float(torch.tensor(case["L"], dtype=real) / float(n[0]))
+
+
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("axes", [(1, 1), (1, 0), (0, 1), (0, 0)])
+def test_gr_filter_matches_reference(axes, real):
+    # grpic::CurrentsFilter's axisymmetric stencil (digital_filter.hpp:196-276)
+    # with and without the axis rows, three passes
+    from oracle.oracle import GROracle
+    g = GridSpec(dim=2, n=(24, 16, 1), order=1, real=real, periodic=(0, 0, 1),
+                 prtl_bc=((1, 1), (3, 3), (0, 0)))
+    o = GROracle(g, 0.9, 1.3, 20.0)
+    r = _ref(g)
+    ja = random_currents(g, 41)
+    jb = ja.clone()
+    for _ in range(3):
+        r.gr_filter_pass(ja, empty_field(g, 3), *axes)
+        o.gr_filter_pass(jb, empty_field(g, 3), *axes)
+    assert torch.equal(ja, jb)
