@@ -1242,6 +1242,9 @@ int pic_gr_filter_currents(pic_ctx* c, const pic_gr_metric* g, void* J, void* bu
   return PIC_OK;
 }
 
+// the sides in Directions<2>::orth order (grpic/fields_bcs.h:242-252): the
+// horizon (-x1) before the axes (-x2, +x2), whose ghost rows then mirror the
+// horizon's copies in the corner cells
 int pic_gr_field_bcs(pic_ctx* c, const pic_gr_metric* g, void* fld, int32_t set_e, int32_t set_b,
                      int32_t nfilter, void* stream) {
   int st = gr_check(c, g);
@@ -1252,12 +1255,12 @@ int pic_gr_field_bcs(pic_ctx* c, const pic_gr_metric* g, void* fld, int32_t set_
   const unsigned b2 = (unsigned)((c->grid.n[1] + 1 + 255) / 256);
   if (is_f64(c)) {
     const auto f = fld_of<double>(c, g);
-    if (g->axis_min || g->axis_max) PIC_KL(pic::k_gr_axis<double><<<b1, 256, 0, s>>>(f, em_view<double>(c, fld), set_e, set_b));
     if (g->horizon) PIC_KL(pic::k_gr_horizon<double><<<b2, 256, 0, s>>>(f, em_view<double>(c, fld), set_e, set_b, nfilter));
+    if (g->axis_min || g->axis_max) PIC_KL(pic::k_gr_axis<double><<<b1, 256, 0, s>>>(f, em_view<double>(c, fld), set_e, set_b));
   } else {
     const auto f = fld_of<float>(c, g);
-    if (g->axis_min || g->axis_max) PIC_KL(pic::k_gr_axis<float><<<b1, 256, 0, s>>>(f, em_view<float>(c, fld), set_e, set_b));
     if (g->horizon) PIC_KL(pic::k_gr_horizon<float><<<b2, 256, 0, s>>>(f, em_view<float>(c, fld), set_e, set_b, nfilter));
+    if (g->axis_min || g->axis_max) PIC_KL(pic::k_gr_axis<float><<<b1, 256, 0, s>>>(f, em_view<float>(c, fld), set_e, set_b));
   }
   return cuda_status(cudaGetLastError());
 }

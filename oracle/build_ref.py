@@ -2,10 +2,12 @@
 INFRASTRUCTURE ONLY).
 
 Compiles oracle/ref_entity.cpp, which includes Entity's kernel headers where
-they lie in the reference checkout (src/kernels/pushers/sr.hpp,
+they lie in the reference checkout (src/kernels/pushers/sr.hpp, gr.hpp,
 currents_deposit.hpp, particle_shapes.hpp, faraday_mink.hpp, ampere_mink.hpp,
-digital_filter.hpp, src/metrics/minkowski.h, src/global/utils/sorting.h and
-what they include), against the host Kokkos shim in oracle/kokkos_shim.
+digital_filter.hpp, faraday_gr.hpp, ampere_gr.hpp, aux_fields_gr.hpp,
+fields_bcs.hpp, src/metrics/minkowski.h, qkerr_schild.h,
+src/global/utils/sorting.h and what they include), against the host Kokkos
+shim in oracle/kokkos_shim.
 Nothing is copied: the headers are read in place through -I. The reference's
 own build system (cmake with Kokkos 5.0.1, an empty submodule here) is not
 used.

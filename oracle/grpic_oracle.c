@@ -563,6 +563,23 @@ void orc_gr_field_bcs(const orc_grid* g, void* fld_, int set_e, int set_b, int a
   real*     F  = (real*)fld_;
   const int ng = g->ng;
   const int N1 = g->n1 + 2 * ng;
+  /* the sides in Directions<2>::orth order (grpic/fields_bcs.h:242-252):
+   * the horizon (-x1) first, then the axes (-x2, +x2) */
+  /* HorizonBoundaries_kernel (fields_bcs.hpp:1188-1240) over i2 in
+   * [i2min, i2max + 1) */
+  if (horizon) {
+    const int i1min = ng;
+    for (int i2 = ng; i2 < g->n2 + ng + 1; ++i2) {
+      if (set_e)
+        for (int i = 0; i <= 2 + nfilter; ++i)
+          for (int c = 0; c < 3; ++c)
+            F[EBI(g, i1min - ng + i, i2, c)] = F[EBI(g, i1min + 1 + nfilter, i2, c)];
+      if (set_b)
+        for (int i = 0; i <= 2 + nfilter; ++i)
+          for (int c = 3; c < 6; ++c)
+            F[EBI(g, i1min - ng + i, i2, c)] = F[EBI(g, i1min + 1 + nfilter, i2, c)];
+    }
+  }
   /* AxisBoundaries_kernel (fields_bcs.hpp:825-868) */
   if (axis_min) {
     const int e = ng;
@@ -594,21 +611,6 @@ void orc_gr_field_bcs(const orc_grid* g, void* fld_, int set_e, int set_b, int a
         F[EBI(g, i1, e + 1, 4)] = -F[EBI(g, i1, e - 1, 4)];
         F[EBI(g, i1, e, 5)]     = F[EBI(g, i1, e - 1, 5)];
       }
-    }
-  }
-  /* HorizonBoundaries_kernel (fields_bcs.hpp:1188-1240) over i2 in
-   * [i2min, i2max + 1) */
-  if (horizon) {
-    const int i1min = ng;
-    for (int i2 = ng; i2 < g->n2 + ng + 1; ++i2) {
-      if (set_e)
-        for (int i = 0; i <= 2 + nfilter; ++i)
-          for (int c = 0; c < 3; ++c)
-            F[EBI(g, i1min - ng + i, i2, c)] = F[EBI(g, i1min + 1 + nfilter, i2, c)];
-      if (set_b)
-        for (int i = 0; i <= 2 + nfilter; ++i)
-          for (int c = 3; c < 6; ++c)
-            F[EBI(g, i1min - ng + i, i2, c)] = F[EBI(g, i1min + 1 + nfilter, i2, c)];
     }
   }
 }

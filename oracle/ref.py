@@ -11,7 +11,7 @@ import ctypes as C
 import torch
 
 from . import build_ref
-from .oracle import Oracle, OrcGrid, OrcSpecies, _p
+from .oracle import GR_NAMES, GR_NQ, GROracle, Oracle, OrcGrid, OrcSpecies, _p
 
 _libs = {}
 
@@ -48,6 +48,18 @@ def lib(real, order):
         L.ref_filter_pass.argtypes = [G, V, V]
         L.ref_filter_pass_axisym.restype = C.c_int
         L.ref_filter_pass_axisym.argtypes = [G, V, V, C.c_int, C.c_int]
+        PD = C.POINTER(C.c_double)
+        PI = C.POINTER(C.c_int)
+        L.ref_gr_metric.restype = C.c_int
+        L.ref_gr_metric.argtypes = [C.c_int, C.c_int, PD, V, C.c_int64, V]
+        L.ref_gr_push.restype = C.c_int
+        L.ref_gr_push.argtypes = [G, PD, S, V, V, D, D, C.c_int, PI, PI]
+        L.ref_gr_field.restype = C.c_int
+        L.ref_gr_field.argtypes = [G, PD, C.c_int, V, V, V, D, C.c_int, C.c_int]
+        L.ref_gr_field_bcs.restype = C.c_int
+        L.ref_gr_field_bcs.argtypes = [G, V] + [C.c_int] * 6
+        L.ref_gr_deposit.restype = C.c_int
+        L.ref_gr_deposit.argtypes = [G, PD, S, V, D]
         L.ref_sort_keys.restype = C.c_int
         L.ref_sort_keys.argtypes = [G, S, C.POINTER(C.c_uint32)]
         _libs[key] = L
@@ -102,3 +114,67 @@ class RefOracle(Oracle):
         _check(self.R.ref_sort_keys(C.byref(self.og), C.byref(s),
                                     C.cast(keys.data_ptr(), C.POINTER(C.c_uint32))))
         return keys[:sp.npart].to(torch.int64) & 0xFFFFFFFF
+
+
+class RefGROracle(GROracle):
+    """The reference's GR kernels (gr::Pusher_kernel, the GRPIC deposit and
+    metric::QKerrSchild<Dim::_2D>) with GROracle's interface; everything else
+    stays the restated oracle's."""
+
+    def __init__(self, g, a, r_min, r_max, th_min=0.0, th_max=3.141592653589793, r0=0.0,
+                 h=0.0):
+        super().__init__(g, a, r_min, r_max, th_min, th_max, r0, h)
+        self.R = lib(g.real, g.order)
+        assert self.R.ref_n_ghosts() == g.ng, "ghost layers differ from the reference build"
+        self.mp = (C.c_double * 7)(r_min, r_max, th_min, th_max, a, r0, h)
+
+    def metric(self, x):
+        x = torch.as_tensor(x, dtype=torch.float64).contiguous()
+        n = x.shape[0]
+        out = torch.empty((n, GR_NQ), dtype=torch.float64)
+        _check(self.R.ref_gr_metric(self.g.n[0], self.g.n[1], self.mp, _p(x), n, _p(out)))
+        return {k: out[:, j] for j, k in enumerate(GR_NAMES)}
+
+    def gr_push(self, sp, em, em0, dt, omegaB0, niter=10, absorb=(1, 1), axis=(1, 1),
+                island=(0, 0)):
+        assert island[1] <= island[0], "the reference has no FP64 island"
+        s = self.species(sp)
+        _check(self.R.ref_gr_push(C.byref(self.og), self.mp, C.byref(s), _p(em), _p(em0), dt,
+                                  omegaB0, niter, (C.c_int * 2)(*absorb), (C.c_int * 2)(*axis)))
+
+    def gr_deposit(self, species, J, dt, island=(0, 0), zero=True):
+        assert island[1] <= island[0], "the reference has no FP64 island"
+        if zero:
+            J.zero_()
+        for sp in species:
+            s = self.species(sp)
+            _check(self.R.ref_gr_deposit(C.byref(self.og), self.mp, C.byref(s), _p(J), dt))
+
+    def _field(self, op, a, b, c, coeff=0.0, axis_min=1, axis_max=1):
+        _check(self.R.ref_gr_field(C.byref(self.og), self.mp, op, _p(a), _p(b), _p(c), coeff,
+                                   axis_min, axis_max))
+
+    def gr_faraday(self, Bin, Bout, E, coeff, axis_min=1):
+        self._field(0, Bin, Bout, E, coeff, axis_min, 1)
+
+    def gr_ampere(self, Din, Dout, H, coeff, axis_min=1, axis_max=1):
+        self._field(1, Din, Dout, H, coeff, axis_min, axis_max)
+
+    def gr_currents_ampere(self, D, J, coeff, axis_min=1, axis_max=1):
+        self._field(2, D, None, J, coeff, axis_min, axis_max)
+
+    def gr_aux_e(self, D, B, E, axis_max=1):
+        self._field(3, D, B, E, 0.0, 1, axis_max)
+
+    def gr_aux_h(self, D, B, H, axis_max=1):
+        self._field(4, D, B, H, 0.0, 1, axis_max)
+
+    def gr_average_db(self, f, f0):
+        self._field(5, f, f0, None)
+
+    def gr_average_j(self, J, J0):
+        self._field(6, J, J0, None)
+
+    def gr_field_bcs(self, fld, set_e, set_b, axis_min=1, axis_max=1, horizon=1, nfilter=0):
+        _check(self.R.ref_gr_field_bcs(C.byref(self.og), _p(fld), int(set_e), int(set_b),
+                                       axis_min, axis_max, horizon, nfilter))

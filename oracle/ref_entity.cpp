@@ -15,12 +15,18 @@
 
 #include "arch/kokkos_aliases.h"
 #include "metrics/minkowski.h"
+#include "metrics/qkerr_schild.h"
 #include "utils/sorting.h"
 
+#include "kernels/ampere_gr.hpp"
 #include "kernels/ampere_mink.hpp"
+#include "kernels/aux_fields_gr.hpp"
+#include "kernels/faraday_gr.hpp"
+#include "kernels/fields_bcs.hpp"
 #include "kernels/currents_deposit.hpp"
 #include "kernels/digital_filter.hpp"
 #include "kernels/faraday_mink.hpp"
+#include "kernels/pushers/gr.hpp"
 #include "kernels/pushers/sr.hpp"
 
 #include "srpic_oracle.h"
@@ -289,6 +295,161 @@ namespace {
                          f);
   }
 
+  // ---- GR: metric::QKerrSchild<Dim::_2D> --------------------------------
+  // mp = { x1min, x1max, x2min, x2max, a, r0, h }
+  using QKS = metric::QKerrSchild<Dim::_2D>;
+  QKS make_qks(int n1, int n2, const double* mp) {
+    std::vector<ncells_t> res { (ncells_t)n1, (ncells_t)n2 };
+    boundaries_t<real_t>  ext { { (real_t)mp[0], (real_t)mp[1] }, { (real_t)mp[2], (real_t)mp[3] } };
+    std::map<std::string, real_t> prm { { "a", (real_t)mp[4] }, { "r0", (real_t)mp[5] },
+                                        { "h", (real_t)mp[6] } };
+    return QKS(res, ext, prm);
+  }
+
+  // grpic::ParticlePush (src/engines/grpic/particle_pusher.h:26-94) for one
+  // species
+  void gr_push(const orc_grid* g, const double* mp, orc_species* sp, const void* em,
+               const void* em0, double dt, double omegaB0, int niter, const int* absorb,
+               const int* axis) {
+    if (sp->npart == 0 || sp->pusher == ORC_PUSHER_NONE) {
+      return;
+    }
+    const QKS                  metric = make_qks(g->n1, g->n2, mp);
+    const kernel::gr::PusherContext ctx { sp->mass,
+                                          sp->charge,
+                                          (real_t)dt,
+                                          (real_t)omegaB0,
+                                          (real_t)1e-6,
+                                          (unsigned short)niter,
+                                          g->n1,
+                                          g->n2,
+                                          1 };
+    boundaries_t<PrtlBC> bcs { { absorb[0] ? PrtlBC::ABSORB : PrtlBC::PERIODIC,
+                                 absorb[1] ? PrtlBC::ABSORB : PrtlBC::PERIODIC },
+                               { axis[0] ? PrtlBC::AXIS : PrtlBC::PERIODIC,
+                                 axis[1] ? PrtlBC::AXIS : PrtlBC::PERIODIC } };
+    const kernel::gr::PusherBoundaries<Dim::_2D> bnd { bcs };
+    ParticleArrays arrays = arrays_of(sp);
+    const auto     DB     = wrap_field<Dim::_2D, 6>(g, em, g->em_s);
+    const auto     DB0    = wrap_field<Dim::_2D, 6>(g, em0, g->em_s);
+    kernel::gr::Pusher_kernel<QKS> k(ctx, bnd, arrays, DB, DB0, metric);
+    if (sp->pusher == ORC_PUSHER_PHOTON) {
+      Kokkos::parallel_for(
+        "ParticlePusher",
+        Kokkos::RangePolicy<Kokkos::DefaultExecutionSpace, kernel::gr::Massless_t>(0, sp->npart),
+        k);
+    } else {
+      Kokkos::parallel_for(
+        "ParticlePusher",
+        Kokkos::RangePolicy<Kokkos::DefaultExecutionSpace, kernel::gr::Massive_t>(0, sp->npart),
+        k);
+    }
+  }
+
+  // grpic::CurrentsDeposit (src/engines/grpic/currents.h:29-73): order 1
+  void gr_deposit(const orc_grid* g, const double* mp, const orc_species* sp, void* J,
+                  double dt) {
+    if (sp->npart == 0 || sp->pusher == ORC_PUSHER_NONE || sp->charge == 0.0f) {
+      return;
+    }
+    const QKS  metric      = make_qks(g->n1, g->n2, mp);
+    auto       cur         = wrap_field<Dim::_2D, 3>(g, J, g->cur_s);
+    auto       scatter_cur = Kokkos::Experimental::create_scatter_view(cur);
+    const auto a           = arrays_of(sp);
+    Kokkos::parallel_for(
+      "CurrentsDeposit",
+      Kokkos::RangePolicy<Kokkos::DefaultExecutionSpace>(0, sp->npart),
+      kernel::DepositCurrents_kernel<SimEngine::GRPIC, QKS>(
+        scatter_cur, a.i1, a.i2, a.i3, a.i1_prev, a.i2_prev, a.i3_prev, a.dx1, a.dx2, a.dx3,
+        a.dx1_prev, a.dx2_prev, a.dx3_prev, a.ux1, a.ux2, a.ux3, array_t<real_t*> {}, a.weight,
+        a.tag, metric, (real_t)sp->charge, (real_t)dt));
+    Kokkos::Experimental::contribute(cur, scatter_cur);
+  }
+
+  boundaries_t<FldsBC> gr_flds_bc(int axis_min, int axis_max, int horizon) {
+    return { { horizon ? FldsBC::HORIZON : FldsBC::FIXED, FldsBC::MATCH },
+             { axis_min ? FldsBC::AXIS : FldsBC::FIXED, axis_max ? FldsBC::AXIS : FldsBC::FIXED } };
+  }
+
+  range_t<Dim::_2D> gr_range(const orc_grid* g, int di1_lo, int di2_hi) {
+    return range_t<Dim::_2D>({ N_GHOSTS - di1_lo, N_GHOSTS },
+                             { N_GHOSTS + (ncells_t)g->n1, N_GHOSTS + (ncells_t)g->n2 + di2_hi });
+  }
+
+  // the GR field kernels as grpic/fieldsolvers.h:79-266 and grpic/utils.h
+  // launch them: op 0 Faraday (a = Bin, b = Bout, c = E), 1 Ampere (a = Din,
+  // b = Dout, c = H), 2 CurrentsAmpere (a = D, c = J), 3 ComputeAuxE (a = D,
+  // b = B, c = E), 4 ComputeAuxH (a = D, b = B, c = H), 5 TimeAverageDB
+  // (a = em, b = em0), 6 TimeAverageJ (a = cur, b = cur0)
+  void gr_field(const orc_grid* g, const double* mp, int op, void* a, void* b, void* c,
+                double coeff, int axis_min, int axis_max) {
+    const QKS  metric = make_qks(g->n1, g->n2, mp);
+    const auto bcs    = gr_flds_bc(axis_min, axis_max, 1);
+    const auto ni2    = (ncells_t)g->n2;
+    auto       em     = [&](void* p) { return wrap_field<Dim::_2D, 6>(g, p, g->em_s); };
+    auto       cu     = [&](void* p) { return wrap_field<Dim::_2D, 3>(g, p, g->cur_s); };
+    switch (op) {
+      case 0:
+        Kokkos::parallel_for("Faraday", gr_range(g, 0, 0),
+                             kernel::gr::Faraday_kernel<QKS>(em(a), em(b), em(c), metric,
+                                                             (real_t)coeff, ni2, bcs));
+        break;
+      case 1:
+        Kokkos::parallel_for("Ampere", gr_range(g, 0, 1),
+                             kernel::gr::Ampere_kernel<QKS>(em(a), em(b), em(c), metric,
+                                                            (real_t)coeff, ni2, bcs));
+        break;
+      case 2:
+        Kokkos::parallel_for("AmpereCurrents", gr_range(g, 0, 1),
+                             kernel::gr::CurrentsAmpere_kernel<QKS>(em(a), cu(c), metric,
+                                                                    (real_t)coeff, ni2, bcs));
+        break;
+      case 3:
+        Kokkos::parallel_for("ComputeAuxE", gr_range(g, 1, axis_max ? 1 : 0),
+                             kernel::gr::ComputeAuxE_kernel<QKS>(em(a), em(b), em(c), metric));
+        break;
+      case 4:
+        Kokkos::parallel_for("ComputeAuxH", gr_range(g, 1, axis_max ? 1 : 0),
+                             kernel::gr::ComputeAuxH_kernel<QKS>(em(a), em(b), em(c), metric));
+        break;
+      case 5:
+        Kokkos::parallel_for("TimeAverageDB", gr_range(g, 0, 0),
+                             kernel::gr::TimeAverageDB_kernel<Dim::_2D>(em(a), em(b)));
+        break;
+      case 6:
+        Kokkos::parallel_for("TimeAverageJ", gr_range(g, 0, 0),
+                             kernel::gr::TimeAverageJ_kernel<Dim::_2D>(cu(a), cu(b)));
+        break;
+      default:
+        break;
+    }
+  }
+
+  // grpic::FieldBoundaries(gr_bc::main) on one field for the horizon and the
+  // axes, in Directions<2>::orth order: -x1 (horizon), -x2, +x2 (axes)
+  // (src/engines/grpic/fields_bcs.h:138-222, 238-252)
+  void gr_field_bcs(const orc_grid* g, void* fld, int set_e, int set_b, int axis_min,
+                    int axis_max, int horizon, int nfilter) {
+    auto         F    = wrap_field<Dim::_2D, 6>(g, fld, g->em_s);
+    const BCTags tags = (set_e ? (BC::Ex1 | BC::Ex2 | BC::Ex3) : 0) |
+                        (set_b ? (BC::Bx1 | BC::Bx2 | BC::Bx3) : 0);
+    const ncells_t i1min = N_GHOSTS, i2min = N_GHOSTS, i2max = N_GHOSTS + (ncells_t)g->n2;
+    if (horizon) {
+      Kokkos::parallel_for("OpenBCFields", range_t<Dim::_1D>(i2min, i2max + 1),
+                           kernel::bc::gr::HorizonBoundaries_kernel<Dim::_2D>(F, i1min, tags,
+                                                                                (unsigned short)nfilter));
+    }
+    const auto n_all1 = (ncells_t)(g->n1 + 2 * g->ng);
+    if (axis_min) {
+      Kokkos::parallel_for("AxisBCFields", n_all1,
+                           kernel::bc::AxisBoundaries_kernel<Dim::_2D, false>(F, i2min, tags));
+    }
+    if (axis_max) {
+      Kokkos::parallel_for("AxisBCFields", n_all1,
+                           kernel::bc::AxisBoundaries_kernel<Dim::_2D, true>(F, i2max, tags));
+    }
+  }
+
   template <class F2, class F3>
   int dispatch(const orc_grid* g, F2&& f2, F3&& f3) {
     if (g->ng != (int)N_GHOSTS) {
@@ -370,6 +531,80 @@ int ref_filter_pass_axisym(const orc_grid* g, void* J, void* buff, int axis_min,
     return -1;
   }
   filter_pass_axisym(g, J, buff, axis_min, axis_max);
+  return 0;
+}
+
+// the QKerrSchild metric functions at n points x (n x 2 code coordinates),
+// out (n x 24) in the oracle's order (grpic_oracle.h: h_11 h_22 h_33 h_13 h11
+// h22 h33 h13 alpha beta1 sqrt_det_h sqrt_det_h_tilde dr_alpha dt_alpha
+// dr_beta1 dt_beta1 dr_h11 dr_h22 dr_h33 dr_h13 dt_h11 dt_h22 dt_h33 dt_h13)
+int ref_gr_metric(int n1, int n2, const double* mp, const double* x, int64_t n, double* out) {
+  const QKS m = make_qks(n1, n2, mp);
+  for (int64_t p = 0; p < n; ++p) {
+    const coord_t<Dim::_2D> xc { (real_t)x[2 * p], (real_t)x[2 * p + 1] };
+    double*                 o = out + 24 * p;
+    o[0]  = m.template h_<1, 1>(xc);
+    o[1]  = m.template h_<2, 2>(xc);
+    o[2]  = m.template h_<3, 3>(xc);
+    o[3]  = m.template h_<1, 3>(xc);
+    o[4]  = m.template h<1, 1>(xc);
+    o[5]  = m.template h<2, 2>(xc);
+    o[6]  = m.template h<3, 3>(xc);
+    o[7]  = m.template h<1, 3>(xc);
+    o[8]  = m.alpha(xc);
+    o[9]  = m.beta1(xc);
+    o[10] = m.sqrt_det_h(xc);
+    o[11] = m.sqrt_det_h_tilde(xc);
+    o[12] = m.dr_alpha(xc);
+    o[13] = m.dt_alpha(xc);
+    o[14] = m.dr_beta1(xc);
+    o[15] = m.dt_beta1(xc);
+    o[16] = m.dr_h11(xc);
+    o[17] = m.dr_h22(xc);
+    o[18] = m.dr_h33(xc);
+    o[19] = m.dr_h13(xc);
+    o[20] = m.dt_h11(xc);
+    o[21] = m.dt_h22(xc);
+    o[22] = m.dt_h33(xc);
+    o[23] = m.dt_h13(xc);
+  }
+  return 0;
+}
+
+int ref_gr_push(const orc_grid* g, const double* mp, orc_species* sp, const void* em,
+                const void* em0, double dt, double omegaB0, int niter, const int* absorb,
+                const int* axis) {
+  if (g->ng != (int)N_GHOSTS || g->dim != 2) {
+    return -1;
+  }
+  gr_push(g, mp, sp, em, em0, dt, omegaB0, niter, absorb, axis);
+  return 0;
+}
+
+int ref_gr_deposit(const orc_grid* g, const double* mp, const orc_species* sp, void* J,
+                   double dt) {
+  if (g->ng != (int)N_GHOSTS || g->dim != 2) {
+    return -1;
+  }
+  gr_deposit(g, mp, sp, J, dt);
+  return 0;
+}
+
+int ref_gr_field(const orc_grid* g, const double* mp, int op, void* a, void* b, void* c,
+                 double coeff, int axis_min, int axis_max) {
+  if (g->ng != (int)N_GHOSTS || g->dim != 2) {
+    return -1;
+  }
+  gr_field(g, mp, op, a, b, c, coeff, axis_min, axis_max);
+  return 0;
+}
+
+int ref_gr_field_bcs(const orc_grid* g, void* fld, int set_e, int set_b, int axis_min,
+                     int axis_max, int horizon, int nfilter) {
+  if (g->ng != (int)N_GHOSTS || g->dim != 2) {
+    return -1;
+  }
+  gr_field_bcs(g, fld, set_e, set_b, axis_min, axis_max, horizon, nfilter);
   return 0;
 }
 
