@@ -313,19 +313,39 @@ struct MultiGather {
   int         n;
 };
 
+// N arrays: every value of a particle is loaded before any is stored, so a
+// thread keeps N loads in flight instead of one
+template <int N>
 __global__ void k_gather_multi(MultiGather g, const int32_t* __restrict__ perm, int64_t np) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np; i += stride) {
     const int64_t j = perm[i];
-    for (int k = 0; k < g.n; ++k) {
+    uint64_t      v[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
       const int64_t jk = j * g.es[k];
-      if (g.esz[k] == 4)
-        ((int32_t*)g.dst[k])[i] = ((const int32_t*)g.src[k])[jk];
-      else if (g.esz[k] == 8)
-        ((int64_t*)g.dst[k])[i] = ((const int64_t*)g.src[k])[jk];
-      else
-        ((int16_t*)g.dst[k])[i] = ((const int16_t*)g.src[k])[jk];
+      if (g.esz[k] == 4)      v[k] = (uint32_t)((const int32_t*)g.src[k])[jk];
+      else if (g.esz[k] == 8) v[k] = (uint64_t)((const int64_t*)g.src[k])[jk];
+      else                    v[k] = (uint16_t)((const int16_t*)g.src[k])[jk];
     }
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      if (g.esz[k] == 4)      ((int32_t*)g.dst[k])[i] = (int32_t)(uint32_t)v[k];
+      else if (g.esz[k] == 8) ((int64_t*)g.dst[k])[i] = (int64_t)v[k];
+      else                    ((int16_t*)g.dst[k])[i] = (int16_t)(uint16_t)v[k];
+    }
+  }
+}
+
+template <int N>
+cudaError_t launch_gather_n(const MultiGather& g, const int32_t* perm, int64_t np, dim3 grid,
+                            cudaStream_t s) {
+  if constexpr (N > kMaxSortArrays) {
+    return cudaErrorInvalidValue;
+  } else {
+    if (g.n != N) return launch_gather_n<N + 1>(g, perm, np, grid, s);
+    PIC_KL(k_gather_multi<N><<<grid, 256, 0, s>>>(g, perm, np));
+    return cudaGetLastError();
   }
 }
 
@@ -412,8 +432,7 @@ cudaError_t sort_apply_all(const GatherSet& g, const int32_t* perm, int64_t n, c
       mc.first_chunk[k + 1] =
         mc.first_chunk[k] + (g.stride[k] == 1 ? (mc.bytes[k] + 15) / 16 : n);
     }
-    PIC_KL(k_gather_multi<<<grid_n(n), 256, 0, s>>>(mg, perm, n));
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = launch_gather_n<1>(mg, perm, n, grid_n(n), s)) != cudaSuccess) return e;
     PIC_KL(k_copy_multi<<<grid_n(mc.first_chunk[g.n]), 256, 0, s>>>(mc));
     return cudaGetLastError();
   }
