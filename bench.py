@@ -210,11 +210,13 @@ def hbm_peak():
     return 6800.0, "fallback"
 
 
-def cpu_sample(w, steps, warmup=1, n=None, sort_interval=0):
+def cpu_sample(w, steps, warmup=1, n=None, sort_interval=0, target_s=10.0):
     """The oracle (the CPU restatement of the reference step, bit-exact with
     the reference's own kernels, OpenMP over all host cores) on a sub-box of
     the workload with the same per-cell content; with sort_interval > 0 it
-    sorts by the reference's cell key as often as the GPU arm sorts."""
+    sorts by the reference's cell key as often as the GPU arm sorts.
+    steps=None times as many steps as fill about target_s seconds, judged
+    from the warm-up steps (2 to 200)."""
     from oracle.oracle import Oracle, lib
     n = n or w["sample_n"]
     g, EB, J, buff, sp = make_setup(w, "cpu", n=n)
@@ -224,8 +226,15 @@ def cpu_sample(w, steps, warmup=1, n=None, sort_interval=0):
     prm = step_prm(g, w, sort_interval)
     o = Oracle(g)
     threads = lib(g.real).orc_max_threads()
-    for k in range(warmup):
+    per = 0.0
+    for k in range(warmup if steps is not None else max(2, warmup)):
+        t0 = time.perf_counter()
         o.step(sp, EB, J, buff, prm, k)
+        per = time.perf_counter() - t0
+        warmup = k + 1
+    if steps is None:
+        # the last warm-up step, past the first touch of the arrays
+        steps = int(min(200, max(2, round(target_s / max(per, 1e-6)))))
     t0 = time.perf_counter()
     for k in range(steps):
         o.step(sp, EB, J, buff, prm, warmup + k)
@@ -467,7 +476,8 @@ def run_ours(args, w):
             del precision[k]
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        cpu = cpu_sample(w, steps=args.cpu_steps)
+        cpu = cpu_sample(w, steps=args.cpu_steps, n=w.get("reference_n"),
+                         sort_interval=args.sort_interval)
     # the metric's adjoint/forward ratio, on the two-stream adjoint problem
     adj = None
     if not args.no_adjoint and world == 1:
@@ -756,7 +766,8 @@ def run_sweep(args, w):
     bytes_pd = npart * BYTES_PER_PARTICLE[w["dim"]] + ncells * BYTES_PER_CELL
     achieved = bytes_pd / (pd_ms / pd_n / 1e3) / 1e9
     peak, peak_src = hbm_peak()
-    cpu = None if args.no_cpu_baseline else cpu_sample(w, steps=args.cpu_steps)
+    cpu = None if args.no_cpu_baseline else cpu_sample(
+        w, steps=args.cpu_steps, n=w.get("reference_n"), sort_interval=args.sort_interval)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -915,7 +926,8 @@ def main():
     ap.add_argument("--cells", type=int, nargs="+", default=None,
                     help="override the grid (smaller cases for profiling)")
     ap.add_argument("--e2e-steps", type=int, default=16)
-    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=None,
+                    help="timed oracle steps of cpu_baseline (default: about 10 s of work)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true",

@@ -28,6 +28,7 @@ constexpr double kSmallAngleGR = 1e-5;
 template <typename M>
 struct QKS {
   M   a, r0, h0, chi_min, eta_min, dchi, deta, dchi_inv, deta_inv;
+  M   x2_small, x2_large;  // code x2 of theta = SMALL_ANGLE_GR and pi - SMALL_ANGLE_GR
   int small_angle;
 
   template <typename N>
@@ -35,6 +36,7 @@ struct QKS {
     QKS<N> o;
     o.a = (N)a, o.r0 = (N)r0, o.h0 = (N)h0, o.chi_min = (N)chi_min, o.eta_min = (N)eta_min;
     o.dchi = (N)dchi, o.deta = (N)deta, o.dchi_inv = (N)dchi_inv, o.deta_inv = (N)deta_inv;
+    o.x2_small = (N)x2_small, o.x2_large = (N)x2_large;
     o.small_angle = small_angle;
     return o;
   }
@@ -51,16 +53,16 @@ struct QKS {
   __device__ M dx_dt(M eta) const {
     if (fabs(h0) <= eps()) return deta;
     return deta * ((M)1 + (M)2 * h0 * (M)kInvPiSqr *
-                            ((M)6 * eta * eta - (M)6 * (M)kPi * eta + (M)kPiSqr));
+                            ((M)6 * (eta * eta) - (M)6 * (M)kPi * eta + (M)kPiSqr));
   }
   __device__ static M eps() { return sizeof(M) == 4 ? (M)1.1920929e-07 : (M)2.220446049250313e-16; }
   // theta clamped to [SMALL_ANGLE_GR, pi - SMALL_ANGLE_GR] in code units
-  // (gr.hpp:338-350; h = 0)
+  // (gr.hpp:352-364); the bounds' code coordinates come from the host
   __device__ M clamp_x2(M x2) const {
     const M th = eta2theta(x2 * deta + eta_min);
     const M small = (M)kSmallAngleGR, large = (M)kPi - small;
-    if (th < small) return (small - eta_min) * deta_inv;
-    if (th >= large) return (large - eta_min) * deta_inv;
+    if (th < small) return x2_small;
+    if (th >= large) return x2_large;
     return x2;
   }
 };

@@ -453,11 +453,13 @@ int pic_srpic_gradient(pic_ctx* ctx, pic_species* sp, pic_species_adjoint* adj,
  * 6-component arrays with the em layout: D (or the auxiliary E) in 0..2, B
  * (or the auxiliary H) in 3..5; currents use the cur layout. Particle
  * boundaries come from pic_grid.prtl_bc: PIC_BC_ABSORB in r, PIC_BC_AXIS in
- * theta. Only h = 0 (theta = eta) is supported.
+ * theta. The polar code coordinate is eta, with theta = eta + 2 h eta
+ * (pi - 2 eta)(pi - eta) / pi^2 (qsph_h = h, 0 <= h < 1; h = 0 gives
+ * theta = eta); x2min and x2max are theta extents.
  * ------------------------------------------------------------------------ */
 typedef struct {
   double  a;              /* spin, 0 <= a < 1 */
-  double  r0, h;          /* qsph_r0, qsph_h (h must be 0) */
+  double  r0, h;          /* qsph_r0, qsph_h (0 <= h < 1) */
   double  x1min, x1max;   /* r extent (r_g) */
   double  x2min, x2max;   /* theta extent */
   int32_t axis_min;       /* field AXIS boundary at theta = x2min */

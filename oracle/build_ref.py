@@ -109,11 +109,15 @@ def build(verbose=False, jobs=None):
 # throw on a mismatch) for the hot path's kernels; they run against the shim
 KERNEL_TESTS = ["deposit", "pusher", "gca_pusher", "ext_force", "prtl_bc", "faraday_mink",
                 "ampere_mink", "digital_filter", "fields_to_phys", "prtls_to_phys", "flds_bc"]
+# the reference's metric tests (tests/metrics/*.cpp): QKerrSchild against
+# Kerr-Schild at h = 0, 0.1 and 0.25, coordinate and vector transformations
+METRIC_TESTS = ["ks-qks", "ks-qks-4d", "coord_trans", "vec_trans"]
 
 
 def build_tests(verbose=False, jobs=None):
-    """Compiles the reference's kernel tests unmodified against the shim into
-    oracle/_ref/tests/<name>_{f32,f64}; returns {(name, tag): path}."""
+    """Compiles the reference's kernel and metric tests unmodified against
+    the shim into oracle/_ref/tests/<name>_{f32,f64}; returns
+    {(name, tag): path}."""
     root = reference_root()
     if root is None:
         return {}
@@ -122,8 +126,9 @@ def build_tests(verbose=False, jobs=None):
     deps = _deps(root)
     aliases = os.path.join(root, "src", "global", "arch", "kokkos_aliases.cpp")
     todo, exes = [], {}
-    for name in KERNEL_TESTS:
-        src = os.path.join(root, "tests", "kernels", name + ".cpp")
+    for name in KERNEL_TESTS + METRIC_TESTS:
+        sub = "kernels" if name in KERNEL_TESTS else "metrics"
+        src = os.path.join(root, "tests", sub, name + ".cpp")
         for tag, defs in (("f32", ["-DSINGLE_PRECISION"]), ("f64", [])):
             target = os.path.join(tdir, f"{name}_{tag}")
             exes[(name, tag)] = target

@@ -13,8 +13,10 @@
 
 #ifdef ORC_SINGLE
 typedef float real;
+#define EPS_REAL FLT_EPSILON
 #else
 typedef double real;
+#define EPS_REAL DBL_EPSILON
 #endif
 
 /* src/global/utils/numeric.h:91-103 */
@@ -62,25 +64,69 @@ typedef double mreal;
 #define M_(fn) fn##_d
 #endif
 
+/* QKerrSchild::eta2theta (qkerr_schild.h:858-869), in real_t */
+static real qks_eta2theta(real h, real eta) {
+  if (fabs((double)h) <= (double)EPS_REAL) return eta;
+  return eta + (real)2 * h * eta * ((real)ORC_PI - (real)2 * eta) * ((real)ORC_PI - eta) *
+                 (real)ORC_INV_PI_SQR;
+}
+
+/* QKerrSchild::theta2eta (qkerr_schild.h:883-912): Cardano's root of the
+ * cubic; h^2, h^3 and theta^2 are real_t products, the rest double */
+static real qks_theta2eta(real h, real theta) {
+  if (fabs((double)h) <= (double)EPS_REAL) return theta;
+  const real   h2 = h * h, h3 = h * h * h, th2 = theta * theta;
+  const double pp = ORC_PI + h * 6.28318530717958647692;
+  const double q  = (4.0 - h) * (pp * pp) - 108.0 * h * ORC_PI * theta + 108.0 * h * th2;
+  const double R  = pow(-9.0 * h2 * (ORC_PI - 2.0 * theta) + 1.73205080756887729352 * sqrt(h3 * q),
+                        1.0 / 3.0);
+  /* pi^(2/3), pi^(1/3), 2^(1/3), (3 pi)^(2/3), 2^(2/3), 3^(1/3) */
+  return (real)(2.14502939711102560008 *
+                (6.0 * 1.46459188756152326302 +
+                 2.0 * 1.2599210498948731647672 * (h - (real)1) * 4.46184094890142313715794 / R +
+                 1.58740105196819947475 * 1.442249570307408382321 * R / h) /
+                12.0);
+}
+
+void orc_gr_convert_x2(const orc_qks* q, int to_code, const double* in, int64_t n, double* out) {
+  const real h = (real)q->h, eta_min = (real)q->eta_min, deta = (real)q->deta;
+  const real deta_inv = (real)q->deta_inv;
+  for (int64_t k = 0; k < n; ++k) {
+    const real x = (real)in[k];
+    out[k] = to_code ? (double)((qks_theta2eta(h, x) - eta_min) * deta_inv)
+                     : (double)qks_eta2theta(h, x * deta + eta_min);
+  }
+}
+
+double orc_qks_theta2eta(double h, double theta) { return qks_theta2eta((real)h, (real)theta); }
+double orc_qks_eta2theta(double h, double eta) { return qks_eta2theta((real)h, (real)eta); }
+
 void orc_qks_init(orc_qks* q, int n1, int n2, double x1min, double x1max, double x2min,
                   double x2max, double a, double r0, double h) {
-  /* QKerrSchild::QKerrSchild (qkerr_schild.h:76-92), in real_t; h = 0 */
-  const real ar = (real)a, r0r = (real)r0;
+  /* QKerrSchild::QKerrSchild (qkerr_schild.h:76-94), in real_t */
+  const real ar = (real)a, r0r = (real)r0, hr = (real)h;
   q->a   = ar;
   q->rh  = (real)((real)1 + (real)sqrt((double)((real)1 - ar * ar)));
   q->r0  = r0r;
-  q->h   = (real)h;
-  const real chi_min = (real)log((double)((real)x1min - r0r));
-  const real eta_min = (real)x2min;
-  const real dchi    = ((real)log((double)((real)x1max - r0r)) - chi_min) / (real)n1;
-  const real deta    = ((real)x2max - eta_min) / (real)n2;
+  q->h   = hr;
+  const real chi_min  = (real)log((double)((real)x1min - r0r));
+  const real eta_min  = qks_theta2eta(hr, (real)x2min);
+  const real dchi     = ((real)log((double)((real)x1max - r0r)) - chi_min) / (real)n1;
+  const real deta     = (qks_theta2eta(hr, (real)x2max) - eta_min) / (real)n2;
+  const real deta_inv = (real)1 / deta;
   q->chi_min  = chi_min;
   q->eta_min  = eta_min;
   q->dchi     = dchi;
   q->deta     = deta;
   q->dchi_inv = (real)1 / dchi;
-  q->deta_inv = (real)1 / deta;
-  q->small_angle = (double)((real)0.5 * deta) < ORC_SMALL_ANGLE;
+  q->deta_inv = deta_inv;
+  q->small_angle = (double)qks_eta2theta(hr, (real)0.5 * deta) < ORC_SMALL_ANGLE;
+  /* gr.hpp:352-364: small is real_t, large = PI - small in double, both
+   * converted through metric.convert<2, Ph, Cd> (qkerr_schild.h:636-640) */
+  const real small = (real)ORC_SMALL_ANGLE_GR;
+  const real large = (real)(ORC_PI - (double)small);
+  q->x2_small = (qks_theta2eta(hr, small) - eta_min) * deta_inv;
+  q->x2_large = (qks_theta2eta(hr, large) - eta_min) * deta_inv;
 }
 
 void orc_gr_metric(const orc_qks* q, const double* x, int64_t n, double* out) {

@@ -27,12 +27,23 @@ extern "C" {
 #endif
 
 /* metric constants in real_t, as QKerrSchild's constructor forms them
- * (qkerr_schild.h:76-92) */
+ * (qkerr_schild.h:76-94), and the code coordinates of the GR pusher's polar
+ * clamp theta in [SMALL_ANGLE_GR, pi - SMALL_ANGLE_GR] (gr.hpp:352-364) */
 typedef struct {
   double a, rh, r0, h;
   double chi_min, eta_min, dchi, deta, dchi_inv, deta_inv;
+  double x2_small, x2_large;
   int    small_angle;
 } orc_qks;
+
+/* theta -> eta and eta -> theta of the angle stretching in real_t
+ * (qkerr_schild.h:858-912) */
+double orc_qks_theta2eta(double h, double theta);
+double orc_qks_eta2theta(double h, double eta);
+
+/* QKerrSchild::convert<2, Ph, Cd> (to_code = 1) or <2, Cd, Ph> (to_code = 0)
+ * at n points (qkerr_schild.h:615-649) */
+void orc_gr_convert_x2(const orc_qks* q, int to_code, const double* in, int64_t n, double* out);
 
 /* QKerrSchild(res, ext, {a, r0, h}) with ext = [[x1min, x1max], [x2min, x2max]] */
 void orc_qks_init(orc_qks* q, int n1, int n2, double x1min, double x1max, double x2min,

@@ -355,7 +355,8 @@ class Oracle:
 # ---------------------------------------------------------------------------
 class OrcQKS(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("a", "rh", "r0", "h", "chi_min", "eta_min", "dchi",
-                                          "deta", "dchi_inv", "deta_inv")] + [
+                                          "deta", "dchi_inv", "deta_inv", "x2_small",
+                                          "x2_large")] + [
         ("small_angle", C.c_int)]
 
 
@@ -372,6 +373,11 @@ def _gr_sigs(L):
     Q, G, S = C.POINTER(OrcQKS), C.POINTER(OrcGrid), C.POINTER(OrcSpecies)
     I2 = C.c_int * 2
     L.orc_qks_init.argtypes = [Q, C.c_int, C.c_int, D, D, D, D, D, D, D]
+    L.orc_qks_theta2eta.restype = D
+    L.orc_qks_theta2eta.argtypes = [D, D]
+    L.orc_qks_eta2theta.restype = D
+    L.orc_qks_eta2theta.argtypes = [D, D]
+    L.orc_gr_convert_x2.argtypes = [Q, C.c_int, V, C.c_int64, V]
     L.orc_gr_metric.argtypes = [Q, V, C.c_int64, V]
     L.orc_gr_transform.argtypes = [Q, C.c_int, V, V, C.c_int64, V]
     L.orc_gr_push.argtypes = [G, Q, S, V, V, D, D, C.c_int, C.c_int, I2, I2, C.c_int, C.c_int]
@@ -404,6 +410,13 @@ class GROracle(Oracle):
         self.L.orc_qks_init(C.byref(self.q), g.n[0], g.n[1], r_min, r_max, th_min, th_max, a,
                             r0, h)
         self.r_min, self.r_max = r_min, r_max
+
+    def convert_x2(self, x, to_code):
+        """theta -> code x2 (to_code) or code x2 -> theta at the points x."""
+        x = torch.as_tensor(x, dtype=torch.float64).contiguous()
+        out = torch.empty_like(x)
+        self.L.orc_gr_convert_x2(C.byref(self.q), int(to_code), _p(x), x.numel(), _p(out))
+        return out
 
     def gr_match(self, fld, target, ds, set_e=1, set_b=1, axis_min=1, axis_max=1):
         self.L.orc_gr_match(C.byref(self.og), C.byref(self.q), _p(fld), _p(target), ds,

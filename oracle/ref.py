@@ -54,6 +54,8 @@ def lib(real, order):
         L.ref_gr_metric.argtypes = [C.c_int, C.c_int, PD, V, C.c_int64, V]
         L.ref_gr_push.restype = C.c_int
         L.ref_gr_push.argtypes = [G, PD, S, V, V, D, D, C.c_int, PI, PI]
+        L.ref_gr_convert_x2.restype = C.c_int
+        L.ref_gr_convert_x2.argtypes = [C.c_int, C.c_int, PD, C.c_int, V, C.c_int64, V]
         L.ref_gr_field.restype = C.c_int
         L.ref_gr_field.argtypes = [G, PD, C.c_int, V, V, V, D, C.c_int, C.c_int]
         L.ref_gr_field_bcs.restype = C.c_int
@@ -134,6 +136,13 @@ class RefGROracle(GROracle):
         out = torch.empty((n, GR_NQ), dtype=torch.float64)
         _check(self.R.ref_gr_metric(self.g.n[0], self.g.n[1], self.mp, _p(x), n, _p(out)))
         return {k: out[:, j] for j, k in enumerate(GR_NAMES)}
+
+    def convert_x2(self, x, to_code):
+        x = torch.as_tensor(x, dtype=torch.float64).contiguous()
+        out = torch.empty_like(x)
+        _check(self.R.ref_gr_convert_x2(self.g.n[0], self.g.n[1], self.mp, int(to_code), _p(x),
+                                        x.numel(), _p(out)))
+        return out
 
     def gr_push(self, sp, em, em0, dt, omegaB0, niter=10, absorb=(1, 1), axis=(1, 1),
                 island=(0, 0)):

@@ -571,6 +571,18 @@ int ref_gr_metric(int n1, int n2, const double* mp, const double* x, int64_t n, 
   return 0;
 }
 
+// metric.convert<2, Ph, Cd> (to_code = 1: theta -> code x2) or
+// convert<2, Cd, Ph> (to_code = 0) at n points (qkerr_schild.h:615-649)
+int ref_gr_convert_x2(int n1, int n2, const double* mp, int to_code, const double* in, int64_t n,
+                      double* out) {
+  const QKS m = make_qks(n1, n2, mp);
+  for (int64_t p = 0; p < n; ++p) {
+    out[p] = to_code ? m.template convert<2, Crd::Ph, Crd::Cd>((real_t)in[p])
+                     : m.template convert<2, Crd::Cd, Crd::Ph>((real_t)in[p]);
+  }
+  return 0;
+}
+
 int ref_gr_push(const orc_grid* g, const double* mp, orc_species* sp, const void* em,
                 const void* em0, double dt, double omegaB0, int niter, const int* absorb,
                 const int* axis) {

@@ -27,14 +27,14 @@ def _lib():
     abi.load()
 
 
-def _setup(real, order=2, n=(48, 32), a=0.95, r_max=20.0):
+def _setup(real, order=2, n=(48, 32), a=0.95, r_max=20.0, h=0.0):
     from entity_gb300.gr import GRContext, GRSpec, gr_grid
     from oracle.oracle import GROracle
     g = gr_grid(n[0], n[1], order=order, real=real)
-    spec = GRSpec(a=a, r_max=r_max)
+    spec = GRSpec(a=a, r_max=r_max, h=h)
     ctx = GRContext(g, spec)
     m = spec.metric()
-    o = GROracle(g, a=a, r_min=m.x1min, r_max=m.x1max, th_min=m.x2min, th_max=m.x2max)
+    o = GROracle(g, a=a, r_min=m.x1min, r_max=m.x1max, th_min=m.x2min, th_max=m.x2max, h=h)
     return g, spec, ctx, o
 
 
@@ -65,8 +65,9 @@ def _X(sp, d):
 
 
 @pytest.mark.parametrize("real", REALS)
-def test_gr_metric_matches_oracle(real):
-    g, spec, ctx, o = _setup(real)
+@pytest.mark.parametrize("h", [0.0, 0.25])
+def test_gr_metric_matches_oracle(real, h):
+    g, spec, ctx, o = _setup(real, h=h)
     gen = torch.Generator().manual_seed(3)
     x = torch.stack([torch.rand(500, generator=gen, dtype=torch.float64) * g.n[0],
                      1.0 + torch.rand(500, generator=gen, dtype=torch.float64) * (g.n[1] - 2)], 1)
@@ -83,8 +84,9 @@ def test_gr_metric_matches_oracle(real):
 @pytest.mark.parametrize("real", REALS)
 @pytest.mark.parametrize("order", [1, 2, 3])
 @pytest.mark.parametrize("pusher", [1, 3])
-def test_gr_push_matches_oracle(real, order, pusher):
-    g, spec, ctx, o = _setup(real, order=order)
+@pytest.mark.parametrize("h", [0.0, 0.25])
+def test_gr_push_matches_oracle(real, order, pusher, h):
+    g, spec, ctx, o = _setup(real, order=order, h=h)
     em, em0 = _rand_fields(g, 1), _rand_fields(g, 2)
     sp = _particles(g, 4000, 5, pusher=pusher)
     dt, omegaB0 = 0.05, 2.0
@@ -228,12 +230,14 @@ def test_gr_field_kernels_match_oracle(real):
 
 
 @pytest.mark.parametrize("real", REALS)
-def test_grpic_step_matches_oracle(real):
+@pytest.mark.parametrize("h", [0.0, 0.25])
+def test_grpic_step_matches_oracle(real, h):
     """Five steps of GRPICEngine::step_forward (with step 0's initialisation)
-    of the vertical-field Wald problem with injected pairs."""
+    of the vertical-field Wald problem with injected pairs, on a grid with
+    theta = eta and on one with stretched polar angles (h = 0.25)."""
     from entity_gb300.gr import gr_step_params, horizon_island, inject_pairs
     from entity_gb300.inputs import empty_field
-    g, spec, ctx, o = _setup(real, order=2, n=(64, 48), r_max=15.0)
+    g, spec, ctx, o = _setup(real, order=2, n=(64, 48), r_max=15.0, h=h)
     em = empty_field(g, 6, "cuda")
     ctx.gr_init_vertical(em)
     fields = [em, torch.zeros_like(em), torch.zeros_like(em), empty_field(g, 3, "cuda"),
@@ -434,3 +438,15 @@ def test_grpic_step_with_match_matches_oracle(real):
         a, b = cpu_fields[k].double(), fields[k].cpu().double()
         scale = float(a.abs().max()) + 1e-30
         assert float((a - b).abs().max()) <= tol * scale, name
+
+
+def test_gr_metric_rejects_h_outside_its_range():
+    """The reference's closed-form theta -> eta is real for 0 <= h < 1."""
+    from entity_gb300 import abi
+    from entity_gb300.gr import GRContext, GRSpec, gr_grid
+    g = gr_grid(16, 16)
+    for h in (-0.2, 1.0):
+        ctx = GRContext(g, GRSpec(h=h))
+        x = torch.zeros(4, 2, dtype=torch.float64, device="cuda")
+        with pytest.raises(abi.PicError):
+            ctx.metric_eval(x)

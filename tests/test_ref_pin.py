@@ -25,6 +25,7 @@ The GPU tests compare the CUDA path with the oracle, so these pins carry over.
 Skipped when the reference checkout is absent (the GPU machine has none).
 """
 import ctypes as C
+import math
 import subprocess
 
 import pytest
@@ -64,7 +65,7 @@ def _assert_species_equal(a, b, dim):
 
 
 @pytest.mark.parametrize("tag", ["f32", "f64"])
-@pytest.mark.parametrize("name", build_ref.KERNEL_TESTS)
+@pytest.mark.parametrize("name", build_ref.KERNEL_TESTS + build_ref.METRIC_TESTS)
 def test_reference_kernel_tests_pass_on_the_shim(name, tag, tmp_path):
     exe = build_ref.build_tests()[(name, tag)]
     # some write logs into their working directory
@@ -335,22 +336,54 @@ def test_gr_filter_matches_reference(axes, real):
     assert torch.equal(ja, jb)
 
 
-def _gr_pair(real, order=2, n=(48, 32)):
-    import math
+# QKerrSchild grids: the full polar range with theta = eta (h = 0), and
+# stretched polar angles (h = 0.25, as the reference's metric tests use, and
+# 0.6) on the full range and on a part of it. The reference's closed-form
+# inverse is real for 0 <= h < 1 only (its square root is of h^3 times a
+# positive factor).
+GR_GRIDS = {"h0": (0.0, math.pi, 0.0), "h025": (0.0, math.pi, 0.25),
+            "h025_part": (0.3, 2.5, 0.25), "h06": (0.0, math.pi, 0.6)}
+
+
+def _gr_pair(real, order=2, n=(48, 32), grid="h0"):
     from oracle.oracle import GROracle
     from oracle.ref import RefGROracle
     g = GridSpec(dim=2, n=(n[0], n[1], 1), order=order, real=real, periodic=(0, 0, 1),
                  prtl_bc=((1, 1), (3, 3), (0, 0)))
     a = 0.95
     rh = 1.0 + math.sqrt(1.0 - a * a)
-    args = (g, a, 0.9 * rh, 20.0)
+    th_min, th_max, h = GR_GRIDS[grid]
+    args = (g, a, 0.9 * rh, 20.0, th_min, th_max, 0.0, h)
     return g, GROracle(*args), RefGROracle(*args)
 
 
 @pytest.mark.parametrize("real", REALS)
-def test_gr_metric_matches_reference(real):
+@pytest.mark.parametrize("grid", sorted(GR_GRIDS))
+def test_gr_metric_constants_and_conversions_match_reference(grid, real):
+    # the constructor's eta_min, deta (through theta2eta, qkerr_schild.h:
+    # 883-912) and the polar conversions both ways
+    g, o, r = _gr_pair(real, grid=grid)
+    th_min, th_max, h = GR_GRIDS[grid]
+    gen = torch.Generator().manual_seed(5)
+    th = th_min + (th_max - th_min) * torch.rand(400, generator=gen, dtype=torch.float64)
+    th = torch.cat([th, torch.tensor([th_min, th_max, 1e-5, math.pi - 1e-5, math.pi / 2])])
+    x2 = torch.rand(400, generator=gen, dtype=torch.float64) * (g.n[1] + 2) - 1
+    assert torch.equal(o.convert_x2(th, True), r.convert_x2(th, True))
+    assert torch.equal(o.convert_x2(x2, False), r.convert_x2(x2, False))
+    if h != 0.0:
+        # the inverse inverts: theta(eta(theta)) to round-off. In float the
+        # closed form cancels near the axes (h^3 is a float product): theta = 0
+        # comes back as about 5e-6 at h = 0.6, in the reference as here.
+        back = o.convert_x2(o.convert_x2(th, True), False)
+        tol = 1e-5 if real == torch.float32 else 1e-12
+        assert float((back - th).abs().max()) <= tol
+
+
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("grid", sorted(GR_GRIDS))
+def test_gr_metric_matches_reference(grid, real):
     # all 24 metric functions of metric::QKerrSchild<Dim::_2D> the GR path uses
-    g, o, r = _gr_pair(real)
+    g, o, r = _gr_pair(real, grid=grid)
     gen = torch.Generator().manual_seed(3)
     x = torch.rand(500, 2, generator=gen, dtype=torch.float64) * torch.tensor([48.0, 32.0])
     mo, mr = o.metric(x), r.metric(x)
@@ -361,13 +394,15 @@ def test_gr_metric_matches_reference(real):
 @pytest.mark.parametrize("real", REALS)
 @pytest.mark.parametrize("order", [1, 2, 3])
 @pytest.mark.parametrize("pusher", [1, 3])
-def test_gr_push_and_deposit_match_reference(pusher, order, real):
+@pytest.mark.parametrize("grid", ["h0", "h025"])
+def test_gr_push_and_deposit_match_reference(grid, pusher, order, real):
     # gr::Pusher_kernel (gr.hpp:71-865): the interpolation, both implicit
-    # iterations, the absorbing radial sides and the axis reflection; then
-    # the GRPIC deposit at order 1 (grpic/currents.h:29-73). The FP64 island
-    # is this build's addition, so the oracle runs without it here.
+    # iterations, the absorbing radial sides and the axis reflection with the
+    # polar clamp; then the GRPIC deposit at order 1 (grpic/currents.h:29-73).
+    # The FP64 island is this build's addition, so the oracle runs without it
+    # here.
     from tests.test_gpu_gr import _particles
-    g, o, r = _gr_pair(real, order)
+    g, o, r = _gr_pair(real, order, grid=grid)
     em = random_fields(g, 3, amp=0.05)
     em0 = random_fields(g, 4, amp=0.05)
     sp = _particles(g, 2000, 7, pusher=pusher, margin=0)
@@ -389,11 +424,12 @@ def test_gr_push_and_deposit_match_reference(pusher, order, real):
 
 
 @pytest.mark.parametrize("real", REALS)
-def test_gr_field_kernels_match_reference(real):
+@pytest.mark.parametrize("grid", ["h0", "h025"])
+def test_gr_field_kernels_match_reference(grid, real):
     # gr::Faraday/Ampere/CurrentsAmpere, ComputeAuxE/H, TimeAverageDB/J and
     # the horizon and axis boundaries, launched over the ranges of
     # grpic/fieldsolvers.h:79-266, grpic/utils.h and grpic/fields_bcs.h
-    g, o, r = _gr_pair(real)
+    g, o, r = _gr_pair(real, grid=grid)
     A, B, E = random_fields(g, 11), random_fields(g, 12), random_fields(g, 13)
     J = random_currents(g, 14)
     cases = {

@@ -37,7 +37,8 @@ def _worker(rank, world, port, out):
 
 def test_reduce_over_ranks_gloo_world2():
     world = 2
-    mgr = mp.Manager()
+    # the manager's server process is started with spawn, as the ranks are
+    mgr = mp.get_context("spawn").Manager()
     out = mgr.dict()
     mp.spawn(_worker, args=(world, _free_port(), out), nprocs=world, join=True)
     assert sorted(out.keys()) == [0, 1]
