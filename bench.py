@@ -272,11 +272,13 @@ def workload_config(w, args, ncells, npart, world):
             "parallelism": f"replicas x{world}"}
 
 
-def precision_twin(w, n, steps, sort_interval, every, timers=False, warm=0):
+def precision_twin(w, n, steps, sort_interval, every, timers=False, warm=0, series_out=None):
     """FP32 and FP64 runs of the same plasma from identical initial states
     (the FP32 inputs converted exactly to FP64), each through pic_srpic_step;
     FP64 field energy and particle moments at checkpoints. Returns the error
-    of the FP32 run against the FP64 run and both throughputs."""
+    of the FP32 run against the FP64 run and both throughputs. With
+    series_out, every checkpoint is also appended to that file as a JSON
+    line as soon as it is taken."""
     import dataclasses
     from entity_gb300.inputs import empty_field
     from entity_gb300.sim import Context, HostPipe
@@ -298,6 +300,9 @@ def precision_twin(w, n, steps, sort_interval, every, timers=False, warm=0):
             m = ctx.particle_moments(sp)
             series.append({"step": k, "field": e2 + b2, "kinetic": m[4], "mgamma": m[0],
                            "p": m[1:4]})
+            if series_out:
+                with open(series_out, "a") as f:
+                    f.write(json.dumps({"precision": tag, **series[-1]}) + "\n")
 
         probe(0)
         evs = []
@@ -754,7 +759,7 @@ def run_sweep(args, w):
     sampler.start()
     launches0 = lib.pic_kernel_launches()
     pr = precision_twin(w, n, total, args.sort_interval, every=args.checkpoint_every or 50,
-                        timers=True, warm=args.warmup)
+                        timers=True, warm=args.warmup, series_out=args.series_out)
     launches = lib.pic_kernel_launches() - launches0
     clocks = sampler.stop()
     phases = pr.pop("_phases_f32")
@@ -937,6 +942,8 @@ def main():
     ap.add_argument("--checkpoint-every", type=int, default=None,
                     help="steps between FP64 diagnostics (sweep3d, default 50) or between "
                          "adjoint checkpoints (adjoint2d, default 20)")
+    ap.add_argument("--series-out", default=None,
+                    help="sweep3d: append each FP32/FP64 checkpoint to this file as it is taken")
     ap.add_argument("--adjoint-steps", type=int, default=None,
                     help="forward steps of the adjoint workload (default 400)")
     args = ap.parse_args()

@@ -165,6 +165,7 @@ SIGNATURES = {
     "pic_field_energy_noalloc": (C.c_int, [C.POINTER(PicGrid), _VP, C.c_double,
                                            C.POINTER(C.c_double), _VP]),
     "pic_get_device_errors": (C.c_int, [_VP, C.POINTER(C.c_int64), C.c_int32, _VP]),
+    "pic_get_wait_timeouts": (C.c_int, [_VP, C.POINTER(C.c_int64), C.c_int32, _VP]),
     "pic_particle_moments": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32,
                                        C.POINTER(C.c_double), _VP]),
     "pic_charge_density": (C.c_int, [_VP, C.POINTER(PicSpecies), C.c_int32, _VP, _VP]),

@@ -344,13 +344,13 @@ int pic_create(const pic_grid* grid, pic_ctx** out) {
   for (int d = 0; d < 3; ++d)
     for (int h = 0; h < 2; ++h)
       c->fbc.kind[d][h] = (d >= grid->dim || grid->fld_periodic[d]) ? PIC_FBC_PERIODIC : PIC_FBC_NONE;
-  if (cudaMalloc((void**)&c->d_err, sizeof(unsigned long long) * 4) != cudaSuccess ||
+  if (cudaMalloc((void**)&c->d_err, sizeof(unsigned long long) * pic::ERR_COUNT) != cudaSuccess ||
       cudaMalloc((void**)&c->d_energy, sizeof(double) * (2 + PIC_NMOMENTS)) != cudaSuccess) {
     if (c->d_err) cudaFree(c->d_err);
     delete c;
     return PIC_ERR_NOMEM;
   }
-  if (cudaMemset(c->d_err, 0, sizeof(unsigned long long) * 4) != cudaSuccess) {
+  if (cudaMemset(c->d_err, 0, sizeof(unsigned long long) * pic::ERR_COUNT) != cudaSuccess) {
     cudaFree(c->d_err);
     cudaFree(c->d_energy);
     delete c;
@@ -756,6 +756,19 @@ int pic_get_device_errors(pic_ctx* c, int64_t out[4], int32_t reset, void* strea
   if (reset) {
     if (cudaMemsetAsync(c->d_err, 0, sizeof(h), s) != cudaSuccess) return PIC_ERR_CUDA;
   }
+  return PIC_OK;
+}
+
+int pic_get_wait_timeouts(pic_ctx* c, int64_t* out, int32_t reset, void* stream) {
+  if (!c || !out) return PIC_ERR_ARG;
+  cudaStream_t       s = strm(stream);
+  unsigned long long h = 0;
+  unsigned long long* d = c->d_err + pic::ERR_WAIT_TIMEOUT;
+  if (cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return PIC_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return PIC_ERR_CUDA;
+  *out = (int64_t)h;
+  if (reset && cudaMemsetAsync(d, 0, sizeof(h), s) != cudaSuccess) return PIC_ERR_CUDA;
   return PIC_OK;
 }
 

@@ -33,7 +33,14 @@ struct Strides {
 };
 
 // device error counters (index meaning documented in entity_pic.h)
-enum ErrIdx { ERR_BAD_TAG = 0, ERR_OUT_OF_GRID = 1, ERR_STENCIL_OUT = 2, ERR_SAMPLER = 3 };
+enum ErrIdx {
+  ERR_BAD_TAG      = 0,
+  ERR_OUT_OF_GRID  = 1,
+  ERR_STENCIL_OUT  = 2,
+  ERR_SAMPLER      = 3,
+  ERR_WAIT_TIMEOUT = 4,  // bounded waits (TMA completion barriers) that ran out
+  ERR_COUNT        = 5
+};
 
 // process-wide count of kernels this library has launched
 void note_launch();

@@ -4,7 +4,10 @@
 // particles of a tile are one contiguous range per species and are read and
 // written back fully coalesced. The CTA
 //   1. stages the E/B window of its tile (tile + interpolation halo + a drift
-//      margin of M cells) in shared memory,
+//      margin of M cells) in shared memory: one TMA box load (all six
+//      components) that runs while the CTA clears its J window and scans its
+//      particles' weights, or a strided copy loop for a window that wraps
+//      across a periodic edge;
 //   2. pushes every particle of the tile (all species) gathering E/B from
 //      shared memory and depositing its current into a shared-memory J window
 //      (tile + deposit halo + margin),
@@ -41,6 +44,7 @@
 #include <type_traits>
 
 #include "push_deposit.cuh"
+#include "tma.cuh"
 
 namespace pic {
 
@@ -155,6 +159,10 @@ struct TiledArgs {
   real               dt, dx, inv_dt;
   int                write_prev;
   unsigned long long* err;
+  // tiled tensor map of EB (x, y, [z], component) with the E-window box;
+  // eb_tma = 0 when the field array does not meet TMA's alignment rules
+  alignas(64) CUtensorMap eb_map;
+  int                eb_tma;
 };
 
 template <int D, int O, typename real>
@@ -169,7 +177,6 @@ struct TiledGeom {
   static constexpr int WJ0 = TX + H::J_LO + H::J_HI;
   static constexpr int WJ1 = TY + H::J_LO + H::J_HI;
   static constexpr int WJ2 = D == 3 ? TZ + H::J_LO + H::J_HI : 1;
-  static constexpr int NE  = WE0 * WE1 * WE2;
   static constexpr int NJ  = WJ0 * WJ1 * WJ2;
   // J window: FixedAcc<real>::WORDS planes of 3 * NJ 32-bit words, in COPIES
   // copies (3D FP32 at order 3: two, one per lane parity) COPY words apart
@@ -179,9 +186,19 @@ struct TiledGeom {
   // the copies start 16 banks apart: one word in both copies falls in
   // two different banks
   static constexpr int    COPY       = WORDS * PLANE + ((16 - (WORDS * PLANE) % 32) + 32) % 32;
+  static constexpr size_t jw_bytes   = 4 * (size_t)(COPIES == 1 ? WORDS * PLANE : COPIES * COPY);
+  // E window rows: a TMA box row is a multiple of 16 bytes and starts on a
+  // 16-byte boundary, so the row is widened to WEX elements and the window
+  // sits R = (x start mod A) elements into it (A elements per 16 bytes)
+  static constexpr int    A          = 16 / (int)sizeof(real);
+  static constexpr int    WEX_TMA    = ((WE0 + A - 1 + A - 1) / A) * A;
+  static constexpr size_t kSmemMax   = 232448 - 128;  // per-CTA limit less the static words
+  static constexpr bool   TMA        = ((sizeof(real) * 6 * (size_t)WEX_TMA * WE1 * WE2 + 127) /
+                                        128) * 128 + jw_bytes <= kSmemMax;
+  static constexpr int    WEX        = TMA ? WEX_TMA : WE0;
+  static constexpr int    NE         = WEX * WE1 * WE2;
   static constexpr size_t eb_bytes   = sizeof(real) * 6 * (size_t)NE;
-  static constexpr size_t smem_bytes = ((eb_bytes + 15) / 16) * 16 +
-                                       4 * (size_t)(COPIES == 1 ? WORDS * PLANE : COPIES * COPY);
+  static constexpr size_t smem_bytes = ((eb_bytes + 127) / 128) * 128 + jw_bytes;
 };
 
 // wraps a ghost-free coordinate of a periodic axis into [0, n)
@@ -192,17 +209,18 @@ __device__ __forceinline__ int wrap_periodic(int x, int n) {
 
 template <int D, int O, typename real>
 __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
-    k_push_deposit_tiled(TiledArgs<real> a) {
+    k_push_deposit_tiled(const __grid_constant__ TiledArgs<real> a) {
   using G               = TiledGeom<D, O, real>;
   using H               = Halo<O>;
   using FA              = FixedAcc<real>;
   constexpr int  NT     = G::NT;
   constexpr int  M      = kDriftMargin;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   real*          EBs = reinterpret_cast<real*>(smem_raw);
-  unsigned*      Jw  = reinterpret_cast<unsigned*>(smem_raw + ((G::eb_bytes + 15) / 16) * 16);
+  unsigned*      Jw  = reinterpret_cast<unsigned*>(smem_raw + ((G::eb_bytes + 127) / 128) * 128);
   real*          Jr  = reinterpret_cast<real*>(Jw);  // real_t accumulation of dense tiles
   __shared__ unsigned int s_qmax;  // bit pattern of the tile's largest |q w| max(1/dt, 1)
+  __shared__ __align__(8) unsigned long long s_bar;  // completion of the E-window load
 
   const int t  = blockIdx.x + a.tile0;
   const int tx = t % a.ntiles[0];
@@ -211,28 +229,55 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
   const int T0[3] = { tx * G::TX, ty * G::TY, tz * G::TZ };
   const int ng    = a.pc.ng;
 
-  // 1. E/B window; reads ghost cells where the window overlaps them and the
-  //    periodic image beyond (zero beyond a non-periodic edge: no valid
-  //    particle's stencil reaches there)
-  for (int idx = threadIdx.x; idx < 6 * G::NE; idx += NT) {
-    int       r  = idx;
-    const int wi = r % G::WE0;
-    r /= G::WE0;
-    const int wj = r % G::WE1;
-    r /= G::WE1;
-    const int wk = r % G::WE2;
-    const int c  = r / G::WE2;
-    int       gc[3] = { T0[0] - H::E_LO + wi, T0[1] - H::E_LO + wj,
-                        D == 3 ? T0[2] - H::E_LO + wk : 0 };
-    bool      inside = true;
+  // 1. E/B window, ghost-inclusive start g0 along each axis; the window's
+  //    rows start R elements into the widened shared rows
+  const int g0[3] = { ng + T0[0] - H::E_LO, ng + T0[1] - H::E_LO,
+                      D == 3 ? ng + T0[2] - H::E_LO : 0 };
+  const int R     = G::TMA ? (g0[0] & (G::A - 1)) : 0;
+  bool      tma   = false;
+  if constexpr (G::TMA) {
+    // one box load covers the window when no periodic axis wraps inside it
+    // (beyond a non-periodic edge the load's zero fill is what the copy
+    // loop writes too)
+    const int we[3] = { G::WE0, G::WE1, G::WE2 };
+    tma = a.eb_tma != 0 && (smem_addr(EBs) & 127u) == 0u;
 #pragma unroll
-    for (int d = 0; d < D; ++d) {
-      if (gc[d] < -ng || gc[d] >= a.pc.n[d] + ng) {
-        if (a.periodic[d]) gc[d] = wrap_periodic(gc[d], a.pc.n[d]);
-        else inside = false;
-      }
+    for (int d = 0; d < D; ++d)
+      if (a.periodic[d] && (g0[d] < 0 || g0[d] + we[d] > a.pc.ext[d])) tma = false;
+  }
+  const unsigned bar = smem_addr(&s_bar);
+  if (tma) {
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      mbar_expect_tx(bar, (unsigned)G::eb_bytes);
+      if constexpr (D == 3) tma_load_4d(smem_addr(EBs), &a.eb_map, bar, g0[0] - R, g0[1], g0[2], 0);
+      else                  tma_load_3d(smem_addr(EBs), &a.eb_map, bar, g0[0] - R, g0[1], 0);
     }
-    EBs[idx] = inside ? a.EB.ld(gc[0] + ng, gc[1] + ng, D == 3 ? gc[2] + ng : 0, c) : (real)0;
+  } else {
+    // reads ghost cells where the window overlaps them and the periodic
+    // image beyond (zero beyond a non-periodic edge: no valid particle's
+    // stencil reaches there)
+    for (int idx = threadIdx.x; idx < 6 * G::WE0 * G::WE1 * G::WE2; idx += NT) {
+      int       r  = idx;
+      const int wi = r % G::WE0;
+      r /= G::WE0;
+      const int wj = r % G::WE1;
+      r /= G::WE1;
+      const int wk = r % G::WE2;
+      const int c  = r / G::WE2;
+      int       gc[3] = { T0[0] - H::E_LO + wi, T0[1] - H::E_LO + wj,
+                          D == 3 ? T0[2] - H::E_LO + wk : 0 };
+      bool      inside = true;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        if (gc[d] < -ng || gc[d] >= a.pc.n[d] + ng) {
+          if (a.periodic[d]) gc[d] = wrap_periodic(gc[d], a.pc.n[d]);
+          else inside = false;
+        }
+      }
+      EBs[R + wi + G::WEX * (wj + G::WE1 * (wk + G::WE2 * c))] =
+          inside ? a.EB.ld(gc[0] + ng, gc[1] + ng, D == 3 ? gc[2] + ng : 0, c) : (real)0;
+    }
   }
   for (int idx = threadIdx.x; idx < (G::COPIES == 1 ? G::WORDS * G::PLANE : G::COPIES * G::COPY);
        idx += NT)
@@ -263,8 +308,16 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
     unscale = (real)ldexp(1.0, ex - b);
   }
 
-  const SmemView<real> ebv{ EBs, ng + T0[0] - H::E_LO, ng + T0[1] - H::E_LO,
-                            D == 3 ? ng + T0[2] - H::E_LO : 0, G::WE0, G::WE0 * G::WE1, G::NE };
+  if (tma) {
+    // every thread waits for the window; a lost wait (the limit ran out on
+    // any thread) abandons the tile on all of them and is counted
+    const bool done = mbar_wait_bounded(bar, 0u);
+    if (__syncthreads_or(!done)) {
+      if (threadIdx.x == 0) atomicAdd(a.err + ERR_WAIT_TIMEOUT, 1ull);
+      return;
+    }
+  }
+  const SmemView<real> ebv{ EBs, g0[0] - R, g0[1], g0[2], G::WEX, G::WEX * G::WE1, G::NE };
   const int joff[3] = { ng + T0[0] - H::J_LO, ng + T0[1] - H::J_LO,
                         D == 3 ? ng + T0[2] - H::J_LO : 0 };
 

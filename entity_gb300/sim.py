@@ -294,6 +294,12 @@ class Context:
         abi.call("pic_get_device_errors", self.h, out, int(reset), _stream_ptr(stream))
         return list(out)
 
+    def wait_timeouts(self, reset=False, stream=None):
+        """Kernel waits that ran out of their iteration limit (0 normally)."""
+        out = C.c_int64(0)
+        abi.call("pic_get_wait_timeouts", self.h, C.byref(out), int(reset), _stream_ptr(stream))
+        return out.value
+
     # --- adjoint ----------------------------------------------------------------
     def gradient(self, species, adjoints, EB, J, buff, prm: abi.PicStepParams, nsteps,
                  checkpoint_every, lamEB, stream=None):

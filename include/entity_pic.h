@@ -301,6 +301,12 @@ int pic_charge_density(pic_ctx* ctx, const pic_species* sp, int32_t nspecies, vo
  * Synchronises the stream. reset != 0 clears the counters. */
 int pic_get_device_errors(pic_ctx* ctx, int64_t out[4], int32_t reset, void* stream);
 
+/* Waits inside kernels that ran out of their iteration limit (the tiled
+ * push/deposit's wait for its TMA field-window load); a tile whose wait ran
+ * out is abandoned and counted here. No counterpart in the reference.
+ * Synchronises the stream. reset != 0 clears the counter. */
+int pic_get_wait_timeouts(pic_ctx* ctx, int64_t* out, int32_t reset, void* stream);
+
 /* Phase timers, the counterpart of timer::Timers with blocking timers
  * (src/global/utils/timer.h:51-148, phases of srpic.hpp:85-187): when enabled,
  * pic_srpic_step records a CUDA event pair on its stream around every phase;

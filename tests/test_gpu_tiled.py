@@ -160,3 +160,31 @@ def test_tiled_falls_back_when_npart_changes():
     torch.cuda.synchronize()
     _assert_particles_equal(c, s, 3)
     _assert_J_close(Jo, Jg, torch.float32)
+
+
+@pytest.mark.parametrize("dim,order,real", [(3, 2, torch.float32), (3, 2, torch.float64),
+                                            (3, 1, torch.float32), (2, 1, torch.float32),
+                                            (2, 2, torch.float64)])
+def test_tma_window_matches_copy_loop(dim, order, real, monkeypatch):
+    """The E/B window staged by the TMA box load equals the one the copy loop
+    stages: particles bit for bit, J to the round-off of the tiles' float
+    flush order. The grid has interior tiles (box load) and edge tiles whose
+    windows wrap (copy loop) in the same launch."""
+    n = (48, 32, 24) if dim == 3 else (96, 64, 1)
+    g = GridSpec(dim=dim, n=n, order=order, real=real)
+    EB = random_fields(g, 19).cuda()
+    ctx, gpu, _ = _tiled_pair(g, [51, 52], temp=0.3)
+    runs = []
+    for no_tma in ("0", "1"):
+        monkeypatch.setenv("ENTITY_PIC_NO_TMA", no_tma)
+        sp = [s.clone() for s in gpu]
+        Jg = empty_field(g, 3, "cuda")
+        ctx.push_deposit(sp, EB, Jg, 0.45, 0.7, g.dx, flags=abi.PIC_PD_WRITE_PREV)
+        ctx.sync_currents(Jg)
+        torch.cuda.synchronize()
+        runs.append((sp, Jg.cpu()))
+    for a, b in zip(runs[0][0], runs[1][0]):
+        _assert_particles_equal(a.to("cpu"), b, dim)
+    _assert_J_close(runs[1][1], runs[0][1].cuda(), real)
+    assert ctx.device_errors() == [0, 0, 0, 0]
+    assert ctx.wait_timeouts() == 0
