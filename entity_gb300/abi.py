@@ -32,6 +32,7 @@ PIC_BC_AXIS = 3
 
 PIC_PD_WRITE_PREV = 1
 PIC_PD_NO_ZERO = 2
+PIC_PD_FLOAT_ATOMICS = 4
 
 PIC_SORT_REMOVE_DEAD = 1
 PIC_SORT_SKIP_PREV = 2

@@ -59,6 +59,11 @@ struct pic_ctx {
   cudaEvent_t                                     gr_fork = nullptr;
   // SR field boundaries (pic_set_field_bcs)
   pic_field_bcs                                   fbc = {};
+  // exact current accumulator of pic_push_deposit (FP32; grown on demand):
+  // 3 x the ghost-inclusive cells of 64-bit totals, and the call's bound
+  long long*                                      jfix       = nullptr;
+  size_t                                          jfix_elems = 0;
+  unsigned*                                       jfix_bound = nullptr;
 };
 
 namespace pic_internal {

@@ -12,6 +12,7 @@
 
 #include "../../include/entity_pic.h"
 #include "ctx_internal.cuh"
+#include "deposit_fixed.cuh"
 #include "fields.cuh"
 #include "moments.cuh"
 #include "push_deposit_tiled.cuh"
@@ -100,8 +101,10 @@ cudaError_t pd_dispatch(const pic_ctx* c, const pic::PDArgs<real>& a, int mode, 
 
 template <typename real>
 int run_pd(pic_ctx* c, const pic_species* sp, const void* EB, void* J, double dt, double omegaB0,
-           double dx, int mode, bool write_prev, cudaStream_t s) {
+           double dx, int mode, bool write_prev, cudaStream_t s,
+           const pic::FixedJ* fj = nullptr) {
   pic::PDArgs<real> a;
+  if (fj) a.fj = *fj;
   a.sp = sptrs(sp);
   for (int d = 0; d < 3; ++d) {
     a.pc.n[d]     = c->grid.n[d];
@@ -177,8 +180,9 @@ pic_species species_tail(const pic_species& sp, int64_t first, int real_bytes) {
 template <typename real>
 int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void* EB, void* J,
               double dt, double omegaB0, double dx, bool write_prev, cudaStream_t s,
-              int64_t tile0 = 0, int64_t tile1 = -1) {
+              int64_t tile0 = 0, int64_t tile1 = -1, const pic::FixedJ* fj = nullptr) {
   pic::TiledArgs<real> a;
+  if (fj) a.fj = *fj;
   a.nsp = (int)sps.size();
   for (int k = 0; k < a.nsp; ++k) {
     const pic_species* sp = sps[k];
@@ -245,6 +249,7 @@ int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void
     pa.err        = a.err;
     pa.list       = a.s[k].ovf;
     pa.list_count = a.s[k].ovf_count;
+    pa.fj         = a.fj;
     e = pd_dispatch<real>(c, pa, pic::MODE_FUSED, false, s);
     if (e != cudaSuccess) return PIC_ERR_CUDA;
   }
@@ -389,6 +394,8 @@ int pic_destroy(pic_ctx* c) {
   if (c->sort_buf) cudaFree(c->sort_buf);
   cudaFree(c->gr_island);
   cudaFree(c->gr_island_cnt);
+  if (c->jfix) cudaFree(c->jfix);
+  if (c->jfix_bound) cudaFree(c->jfix_bound);
   if (c->gr_fork) cudaEventDestroy(c->gr_fork);
   for (auto e : c->gr_join) cudaEventDestroy(e);
   for (auto q : c->gr_side) cudaStreamDestroy(q);
@@ -548,6 +555,56 @@ int pic_deposit(pic_ctx* c, const pic_species* sp, int32_t nspecies, void* J, do
   return PIC_OK;
 }
 
+// Arms the exact current accumulator for one FP32 pic_push_deposit call over
+// the species that deposit: clears the totals and the bound, then bounds
+// |q w| over their particles. Returns false when the accumulator cannot be
+// allocated (the call then deposits with float atomics).
+bool arm_fixed_J(pic_ctx* c, const pic_species* sp, int32_t nspecies, double dt, cudaStream_t s,
+                 pic::FixedJ* fj) {
+  const int    dim = c->grid.dim, ng = c->grid.ng;
+  const int    e0 = c->grid.n[0] + 2 * ng, e1 = dim >= 2 ? c->grid.n[1] + 2 * ng : 1;
+  const int    e2 = dim >= 3 ? c->grid.n[2] + 2 * ng : 1;
+  const size_t elems = (size_t)3 * e0 * e1 * e2;
+  if (c->jfix_elems < elems) {
+    if (c->jfix) cudaFree(c->jfix);
+    c->jfix       = nullptr;
+    c->jfix_elems = 0;
+    if (cudaMalloc((void**)&c->jfix, sizeof(long long) * elems) != cudaSuccess) {
+      cudaGetLastError();
+      c->jfix = nullptr;
+      return false;
+    }
+    c->jfix_elems = elems;
+  }
+  if (!c->jfix_bound && cudaMalloc((void**)&c->jfix_bound, sizeof(unsigned)) != cudaSuccess) {
+    cudaGetLastError();
+    c->jfix_bound = nullptr;
+    return false;
+  }
+  if (cudaMemsetAsync(c->jfix, 0, sizeof(long long) * elems, s) != cudaSuccess ||
+      cudaMemsetAsync(c->jfix_bound, 0, sizeof(unsigned), s) != cudaSuccess)
+    return false;
+  int64_t ntot = 0;
+  for (int k = 0; k < nspecies; ++k) {
+    const pic_species* q = sp + k;
+    if (q->pusher == PIC_PUSHER_NONE || q->npart == 0 || q->charge == 0.0f) continue;
+    ntot += q->npart;
+    if (pic::launch_weight_bound((const float*)q->weight, q->npart, std::fabs(q->charge),
+                                 c->jfix_bound, s) != cudaSuccess)
+      return false;
+  }
+  int lg = 0;
+  while (lg < 62 && (int64_t(1) << lg) < ntot + 1) ++lg;
+  fj->p         = c->jfix;
+  fj->s1        = e0;
+  fj->s2        = (int64_t)e0 * e1;
+  fj->s3        = (int64_t)e0 * e1 * e2;
+  fj->bound     = c->jfix_bound;
+  fj->dt_factor = std::fmax(1.f / (float)dt, 1.f);  // the kernels' inv_dt
+  fj->bits      = std::min(34, 62 - lg);
+  return fj->bits >= 8;
+}
+
 int pic_push_deposit(pic_ctx* c, const pic_species* sp, int32_t nspecies, const void* EB, void* J,
                      double dt, double omegaB0, double dx, uint32_t flags, void* stream) {
   if (!c || !EB || !J || nspecies < 0 || (nspecies > 0 && !sp)) return PIC_ERR_ARG;
@@ -559,10 +616,15 @@ int pic_push_deposit(pic_ctx* c, const pic_species* sp, int32_t nspecies, const 
       return PIC_ERR_ARG;
   }
   int st = PIC_OK;
-  if (!(flags & PIC_PD_NO_ZERO)) {
+  // FP32: deposit into the exact accumulator, then J (+)= its totals once
+  pic::FixedJ fj;
+  const bool  exact = !is_f64(c) && !(flags & PIC_PD_FLOAT_ATOMICS) &&
+                     arm_fixed_J(c, sp, nspecies, dt, strm(stream), &fj);
+  if (!(flags & PIC_PD_NO_ZERO) && !exact) {
     st = is_f64(c) ? zero_J<double>(c, J, strm(stream)) : zero_J<float>(c, J, strm(stream));
     if (st != PIC_OK) return st;
   }
+  const pic::FixedJ* fjp = exact ? &fj : nullptr;
   // species with a valid tile binning (PIC_SORT_TILED) go through the tiled
   // kernel together; the rest, and any particles beyond a binned prefix,
   // through the per-particle kernel
@@ -584,7 +646,8 @@ int pic_push_deposit(pic_ctx* c, const pic_species* sp, int32_t nspecies, const 
   }
   if (!tiled.empty()) {
     st = is_f64(c) ? run_tiled<double>(c, tiled, EB, J, dt, omegaB0, dx, write_prev, strm(stream))
-                   : run_tiled<float>(c, tiled, EB, J, dt, omegaB0, dx, write_prev, strm(stream));
+                   : run_tiled<float>(c, tiled, EB, J, dt, omegaB0, dx, write_prev, strm(stream),
+                                      0, -1, fjp);
     if (st != PIC_OK) return st;
   }
   for (const pic_species& rs : rest) {
@@ -595,14 +658,21 @@ int pic_push_deposit(pic_ctx* c, const pic_species* sp, int32_t nspecies, const 
       // push-only kernels always store prev; without prev arrays use the
       // fused kernel with zero charge semantics instead
       st = is_f64(c) ? run_pd<double>(c, s, EB, J, dt, omegaB0, dx, pic::MODE_FUSED, false, strm(stream))
-                     : run_pd<float>(c, s, EB, J, dt, omegaB0, dx, pic::MODE_FUSED, false, strm(stream));
+                     : run_pd<float>(c, s, EB, J, dt, omegaB0, dx, pic::MODE_FUSED, false, strm(stream), fjp);
     } else {
       st = is_f64(c) ? run_pd<double>(c, s, EB, J, dt, omegaB0, dx, mode, write_prev, strm(stream))
-                     : run_pd<float>(c, s, EB, J, dt, omegaB0, dx, mode, write_prev, strm(stream));
+                     : run_pd<float>(c, s, EB, J, dt, omegaB0, dx, mode, write_prev, strm(stream), fjp);
     }
     if (st != PIC_OK) return st;
   }
-  return PIC_OK;
+  if (exact) {
+    const int ext[3] = { c->grid.n[0] + 2 * c->grid.ng,
+                         c->grid.dim >= 2 ? c->grid.n[1] + 2 * c->grid.ng : 1,
+                         c->grid.dim >= 3 ? c->grid.n[2] + 2 * c->grid.ng : 1 };
+    st = cuda_status(pic::launch_fixed_to_real(fj, cur_view<float>(c, J), ext,
+                                               !(flags & PIC_PD_NO_ZERO), strm(stream)));
+  }
+  return st;
 }
 
 int pic_tile_offsets(pic_ctx* c, const pic_species* sp, int32_t* out, int64_t cap,

@@ -8,6 +8,7 @@
 // prev-arrays never round-trip through HBM.
 #pragma once
 
+#include "deposit_fixed.cuh"
 #include "pic_common.cuh"
 
 namespace pic {
@@ -28,6 +29,8 @@ struct PDArgs {
   // *list_count of them (a device counter)
   const int32_t*  list       = nullptr;
   const unsigned* list_count = nullptr;
+  // optional (FP32): deposit into the exact 64-bit accumulator instead of J
+  FixedJ          fj;
 };
 
 template <int D, int O, typename real, int MODE, bool PHOTON>
@@ -40,6 +43,11 @@ __global__ void __launch_bounds__(256) k_push_deposit(PDArgs<real> a) {
   float*        da[3]  = { a.sp.dx1, a.sp.dx2, a.sp.dx3 };
   float*        dpa[3] = { a.sp.dx1p, a.sp.dx2p, a.sp.dx3p };
   const int64_t n = a.list ? (int64_t)*a.list_count : a.sp.npart;
+  // scale of the exact accumulator: contributions in units of 2^(ex - bits)
+  float fj_scale = 0.f;
+  if constexpr (sizeof(real) == 4 && MODE != MODE_PUSH) {
+    if (a.fj.p) fj_scale = ldexpf(1.f, a.fj.bits - a.fj.exponent());
+  }
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += stride) {
     const int64_t p = a.list ? (int64_t)a.list[t] : t;
     Prtl<real>    q;
@@ -111,11 +119,25 @@ __global__ void __launch_bounds__(256) k_push_deposit(PDArgs<real> a) {
     }
     if constexpr (MODE != MODE_PUSH) {
       if (q.tag == PIC_TAG_DEAD) continue;
-      const FieldView<real>& J = a.J;
-      const bool ok = deposit_particle<D, O, real>(q, w[p], a.charge, a.inv_dt, a.dx, a.pc.ng,
-                                                   a.pc.ext, [&](int i, int j, int k, int c, real v) {
-                                                     atomicAdd(J.p + J.idx(i, j, k, c), v);
-                                                   });
+      const FieldView<real>& J    = a.J;
+      auto                   to_J = [&](int i, int j, int k, int c, real v) {
+        atomicAdd(J.p + J.idx(i, j, k, c), v);
+      };
+      bool ok;
+      if constexpr (sizeof(real) == 4) {
+        if (a.fj.p)
+          ok = deposit_particle<D, O, real>(q, w[p], a.charge, a.inv_dt, a.dx, a.pc.ng, a.pc.ext,
+                                            [&](int i, int j, int k, int c, real v) {
+                                              a.fj.add_units(i, j, k, c,
+                                                             __float2ll_rn(v * fj_scale));
+                                            });
+        else
+          ok = deposit_particle<D, O, real>(q, w[p], a.charge, a.inv_dt, a.dx, a.pc.ng, a.pc.ext,
+                                            to_J);
+      } else {
+        ok = deposit_particle<D, O, real>(q, w[p], a.charge, a.inv_dt, a.dx, a.pc.ng, a.pc.ext,
+                                          to_J);
+      }
       if (!ok) atomicAdd(a.err + ERR_STENCIL_OUT, 1ull);
     }
   }

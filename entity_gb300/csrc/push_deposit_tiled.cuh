@@ -163,6 +163,9 @@ struct TiledArgs {
   // eb_tma = 0 when the field array does not meet TMA's alignment rules
   alignas(64) CUtensorMap eb_map;
   int                eb_tma;
+  // FP32: the exact 64-bit accumulator the tile sums are flushed into (null:
+  // float atomics into J)
+  FixedJ             fj;
 };
 
 template <int D, int O, typename real>
@@ -286,13 +289,16 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
   // particle count (an upper bound on the additions any cell receives)
   if (threadIdx.x == 0) s_qmax = 0u;
   __syncthreads();
-  float   qmax = 0.f;
-  int64_t ntile = 0;
+  // (with the exact global accumulator the bound is the call's, known already)
+  const bool global_unit = sizeof(real) == 4 && a.fj.p != nullptr;
+  float      qmax = 0.f;
+  int64_t    ntile = 0;
   for (int s = 0; s < a.nsp; ++s) {
     const real*   w  = (const real*)a.s[s].sp.w;
     const float   qs = fabsf((float)a.s[s].charge);
     const int64_t lo = a.s[s].tile_start[t], hi = a.s[s].tile_start[t + 1];
     ntile += hi - lo;
+    if (global_unit) continue;
     for (int64_t p = lo + threadIdx.x; p < hi; p += NT) qmax = fmaxf(qmax, fabsf((float)w[p]) * qs);
   }
   qmax *= fmaxf((float)a.inv_dt, 1.f);
@@ -300,13 +306,17 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
   __syncthreads();
   const bool fixed = ntile <= FA::NMAX;
   real       scale = 1, unscale = 1;
-  {
-    int ex = 0;
+  int        ex = 0, b = FA::bits(ntile);
+  if (global_unit) {
+    // the call's bound, and no more bits than the global unit has, so that
+    // a tile total becomes global units by a left shift
+    ex = a.fj.exponent();
+    b  = min(b, a.fj.bits);
+  } else {
     frexpf(__uint_as_float(s_qmax) * 1.0000002f, &ex);  // |contribution| < 2^ex
-    const int b = FA::bits(ntile);
-    scale   = (real)ldexp(1.0, b - ex);
-    unscale = (real)ldexp(1.0, ex - b);
   }
+  scale   = (real)ldexp(1.0, b - ex);
+  unscale = (real)ldexp(1.0, ex - b);
 
   if (tma) {
     // every thread waits for the window; a lost wait (the limit ran out on
@@ -435,7 +445,8 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
 
   // 3. flush the J window (periodic images folded onto active cells)
   for (int idx = threadIdx.x; idx < 3 * G::NJ; idx += NT) {
-    real v;
+    real      v = 0;
+    long long units = 0;  // the entry in global units (exact accumulator)
     if (fixed) {
       long long t = 0;
       bool      any = false;
@@ -448,10 +459,12 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
         }
       }
       if (!any) continue;
-      v = FA::to_real(t, unscale);
+      if (global_unit) units = (long long)((unsigned long long)t << (a.fj.bits - b));
+      else             v = FA::to_real(t, unscale);
     } else {
       v = Jr[idx];
       if (v == (real)0) continue;
+      if (global_unit) units = __float2ll_rn((float)v * ldexpf(1.f, a.fj.bits - ex));
     }
     int       r  = idx;
     const int wi = r % G::WJ0;
@@ -472,6 +485,12 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
       }
     }
     if (inside) {
+      if constexpr (sizeof(real) == 4) {
+        if (global_unit) {
+          a.fj.add_units(gc[0] + ng, gc[1] + ng, D == 3 ? gc[2] + ng : 0, c, units);
+          continue;
+        }
+      }
       atomicAdd(a.J.p + a.J.idx(gc[0] + ng, gc[1] + ng, D == 3 ? gc[2] + ng : 0, c), v);
     } else {
       atomicAdd(a.err + ERR_STENCIL_OUT, 1ull);

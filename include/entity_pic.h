@@ -55,8 +55,10 @@ extern "C" {
 #define PIC_BC_AXIS 3
 
 /* push/deposit flags */
-#define PIC_PD_WRITE_PREV 1u /* store i*_prev / dx*_prev like the reference pusher */
-#define PIC_PD_NO_ZERO 2u    /* do not zero J before depositing */
+#define PIC_PD_WRITE_PREV 1u    /* store i*_prev / dx*_prev like the reference pusher */
+#define PIC_PD_NO_ZERO 2u       /* do not zero J before depositing */
+#define PIC_PD_FLOAT_ATOMICS 4u /* FP32: add contributions to J with float atomics in
+                                   arrival order instead of the exact accumulation */
 
 /* sort flags */
 #define PIC_SORT_REMOVE_DEAD 1u /* Particles::RemoveDead before the spatial sort */
@@ -193,7 +195,14 @@ int pic_deposit(pic_ctx* ctx, const pic_species* sp, int32_t nspecies, void* J, 
 /* Fused ParticlePush + CurrentsDeposit for nspecies species: one pass reads
  * each particle once, moves it and deposits its current; the previous
  * position stays in registers (written out only with PIC_PD_WRITE_PREV).
- * J is zeroed first unless PIC_PD_NO_ZERO. */
+ * J is zeroed first unless PIC_PD_NO_ZERO.
+ * FP32 grids accumulate the call's contributions exactly: each is a multiple
+ * of 2^(e - b) (2^e bounds |q w| max(1/dt, 1) over the call's particles,
+ * b = min(34, 62 - ceil(log2(N + 1))) for N particles), summed as 64-bit
+ * integers in a context-owned buffer and converted to float once per entry,
+ * so J does not depend on the order of the additions and repeats bit for bit
+ * from run to run. The reference's device build adds floats atomically in
+ * arrival order (ScatterView); PIC_PD_FLOAT_ATOMICS does the same here. */
 int pic_push_deposit(pic_ctx* ctx, const pic_species* sp, int32_t nspecies, const void* EB,
                      void* J, double dt, double omegaB0, double dx, uint32_t flags,
                      void* stream);
@@ -211,8 +220,8 @@ int pic_tile_offsets(pic_ctx* ctx, const pic_species* sp, int32_t* out, int64_t 
  * binned species (Boris or Vay): the tiled kernel over those tiles, then the
  * per-particle kernel over the ones it deferred. J is zeroed first unless
  * PIC_PD_NO_ZERO. Covering every tile once, in any number of calls, gives the
- * same particles and the same J (up to the order of the J additions) as one
- * pic_push_deposit call. Dead particles after the alive prefix are not
+ * same particles and the same J (up to the order of the J additions: these
+ * calls add to J with float atomics) as one pic_push_deposit call. Dead particles after the alive prefix are not
  * visited. PIC_ERR_UNSUPPORTED without a valid binning. No reference
  * counterpart: it lets a caller push part of a species while the rest is
  * still being copied in. */

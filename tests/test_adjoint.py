@@ -122,6 +122,15 @@ def test_gradient_fp32_against_fd_and_fp64():
     assert L32 == pytest.approx(L64, rel=1e-4)
 
 
+@pytest.mark.parametrize("real", [torch.float32, torch.float64])
+def test_amplitude_gradient_at_the_stated_step(real):
+    """At h = 1e-4 the amplitude gradient meets the 1e-3 bar: the amplitude
+    enters through the weights and the initial Gauss field, not through the
+    float in-cell offsets whose rounding floors the drift quotient there."""
+    L, gb, ga = _grad(real)
+    assert ga == pytest.approx(_fd_gpu(real, "amp", 1e-4), rel=1e-3)
+
+
 def test_checkpoint_interval_does_not_change_the_gradient():
     ref = _grad(torch.float64, every=STEPS)
     for every in (1, 7, 16):

@@ -12,7 +12,7 @@ import torch
 from entity_gb300 import abi
 from entity_gb300.inputs import GridSpec, empty_field, make_species
 from entity_gb300.sim import Context
-from tests.helpers import random_fields
+from tests.helpers import random_currents, random_fields
 from tests.test_gpu_parity import J_TOL, _assert_J_close, _assert_particles_equal
 
 pytestmark = pytest.mark.gpu
@@ -188,3 +188,51 @@ def test_tma_window_matches_copy_loop(dim, order, real, monkeypatch):
     _assert_J_close(runs[1][1], runs[0][1].cuda(), real)
     assert ctx.device_errors() == [0, 0, 0, 0]
     assert ctx.wait_timeouts() == 0
+
+
+@pytest.mark.parametrize("dim,order", [(3, 2), (3, 3), (2, 1)])
+def test_exact_current_accumulation_repeats_bit_for_bit(dim, order):
+    """FP32 J from the exact 64-bit accumulation is the same in every run,
+    whatever order the tiles, the per-particle drain of the particles that
+    left their tile's margin and an unsorted species add in; it agrees with
+    the float-atomic deposit to round-off, and the particles are identical."""
+    n = (40, 24, 16) if dim == 3 else (96, 64, 1)
+    g = GridSpec(dim=dim, n=n, order=order, real=torch.float32)
+    EB = random_fields(g, 23, amp=0.1).cuda()
+    ctx, gpu, _ = _tiled_pair(g, [61, 62], temp=2.0, beta=0.5)
+    # a third species the sort never binned: the per-particle kernel
+    gpu.append(make_species(g, 3, 0.5, 0.1, 63, charge=-1.0, index=3).to("cuda"))
+    runs = []
+    for flags in (0, 0, abi.PIC_PD_FLOAT_ATOMICS):
+        sp = [s.clone() for s in gpu]
+        Js = []
+        for _ in range(4):  # no re-sort: particles drift past the margin
+            Jg = empty_field(g, 3, "cuda")
+            ctx.push_deposit(sp, EB, Jg, 0.45, 0.7, g.dx,
+                             flags=abi.PIC_PD_WRITE_PREV | flags)
+            Js.append(Jg)
+        torch.cuda.synchronize()
+        runs.append((sp, Js))
+    for Ja, Jb, Jf in zip(runs[0][1], runs[1][1], runs[2][1]):
+        assert torch.equal(Ja, Jb)
+        _assert_J_close(Jf.cpu(), Ja, torch.float32)
+    for a, b in zip(runs[0][0], runs[2][0]):
+        _assert_particles_equal(a.to("cpu"), b, dim)
+    assert ctx.device_errors() == [0, 0, 0, 0]
+
+
+def test_exact_current_accumulation_adds_to_J():
+    """With PIC_PD_NO_ZERO the call adds its float totals to J: the same as
+    depositing into zeros and adding in float."""
+    g = GridSpec(dim=3, n=(24, 16, 16), order=2, real=torch.float32)
+    EB = random_fields(g, 29, amp=0.1).cuda()
+    ctx, gpu, _ = _tiled_pair(g, [71, 72], temp=0.3)
+    J0 = random_currents(g, 30).cuda()
+    Ja = J0.clone()
+    ctx.push_deposit([s.clone() for s in gpu], EB, Ja, 0.45, 0.7, g.dx,
+                     flags=abi.PIC_PD_WRITE_PREV | abi.PIC_PD_NO_ZERO)
+    Jz = empty_field(g, 3, "cuda")
+    ctx.push_deposit([s.clone() for s in gpu], EB, Jz, 0.45, 0.7, g.dx,
+                     flags=abi.PIC_PD_WRITE_PREV)
+    torch.cuda.synchronize()
+    assert torch.equal(Ja, J0 + Jz)
