@@ -390,6 +390,8 @@ def run_ours(args, w):
 
     g, EB, J, buff, sp = make_setup(w, "cuda", n=args.cells)
     prm = step_prm(g, w, args.sort_interval, sort_tiled=not args.reference_sort_key)
+    if args.float_atomics:
+        prm.deposit_flags = abi.PIC_PD_FLOAT_ATOMICS
     ctx = Context(g)
     npart = sum(s.npart for s in sp)
     torch.cuda.synchronize()
@@ -494,6 +496,8 @@ def run_ours(args, w):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(w, args, g.ncells(), npart, world),
         "sort_key": "reference cell key" if args.reference_sort_key else "tile-major",
+        "current_sum": ("float atomics" if args.float_atomics
+                        else "exact (64-bit fixed point, order-independent)"),
         "ns_per_particle_step": 1e9 / (value / world),
         "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in phases.items()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -942,6 +946,8 @@ def main():
     ap.add_argument("--checkpoint-every", type=int, default=None,
                     help="steps between FP64 diagnostics (sweep3d, default 50) or between "
                          "adjoint checkpoints (adjoint2d, default 20)")
+    ap.add_argument("--float-atomics", action="store_true",
+                    help="deposit with float atomics instead of the exact accumulation")
     ap.add_argument("--series-out", default=None,
                     help="sweep3d: append each FP32/FP64 checkpoint to this file as it is taken")
     ap.add_argument("--adjoint-steps", type=int, default=None,

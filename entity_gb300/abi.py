@@ -128,7 +128,7 @@ class PicStepParams(C.Structure):
         ("q0", C.c_double), ("B0", C.c_double), ("V0", C.c_double), ("ppc0", C.c_double),
         ("nfilter", C.c_int32), ("sort_interval", C.c_int32), ("clear_interval", C.c_int32),
         ("fieldsolver_enabled", C.c_int32), ("deposit_enabled", C.c_int32),
-        ("write_prev", C.c_int32), ("sort_tiled", C.c_int32),
+        ("write_prev", C.c_int32), ("sort_tiled", C.c_int32), ("deposit_flags", C.c_int32),
     ]
 
 

@@ -421,7 +421,8 @@ int pic_srpic_step_host(pic_ctx* ctx, pic_host_pipe* p, pic_species* hsp, pic_sp
   const double   dt     = f64 ? prm->dt : (double)(float)prm->dt;
   const double   wB     = f64 ? prm->omegaB0 : (double)(float)prm->omegaB0;
   const double   dxc    = f64 ? prm->dx : (double)(float)prm->dx;
-  const uint32_t fl     = prm->write_prev ? PIC_PD_WRITE_PREV : 0u;
+  const uint32_t fl     = (prm->write_prev ? PIC_PD_WRITE_PREV : 0u) |
+                          ((uint32_t)prm->deposit_flags & PIC_PD_FLOAT_ATOMICS);
   bool           zeroed = false;
   if (dep && nspecies == 0) {
     PIC_TRY(pic_push_deposit(ctx, nullptr, 0, dEB, dJ, dt, wB, dxc, fl, stream));

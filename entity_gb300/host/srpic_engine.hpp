@@ -66,7 +66,8 @@ int AmpereWithCurrents(Domain& dom, const pic_step_params& p, real fraction, boo
 // srpic::ParticlePush + srpic::CurrentsDeposit, fused
 template <typename real>
 int PushDeposit(Domain& dom, const pic_step_params& p, bool deposit, void* stream) {
-  const uint32_t flags = p.write_prev ? PIC_PD_WRITE_PREV : 0u;
+  const uint32_t flags = (p.write_prev ? PIC_PD_WRITE_PREV : 0u) |
+                         ((uint32_t)p.deposit_flags & PIC_PD_FLOAT_ATOMICS);
   if (deposit) {
     return pic_push_deposit(dom.ctx, dom.species.data(), (int32_t)dom.species.size(), dom.EB, dom.J,
                             (double)(real)p.dt, (double)(real)p.omegaB0, (double)(real)p.dx,

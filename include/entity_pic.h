@@ -355,6 +355,7 @@ typedef struct {
   int32_t deposit_enabled;
   int32_t write_prev;
   int32_t sort_tiled; /* spatial sorts use PIC_SORT_TILED */
+  int32_t deposit_flags; /* extra pic_push_deposit flags: PIC_PD_FLOAT_ATOMICS or 0 */
 } pic_step_params;
 
 int pic_srpic_step(pic_ctx* ctx, pic_species* sp, int32_t nspecies, void* EB, void* J,

@@ -101,3 +101,38 @@ def test_product_library_does_not_link_the_oracle(lib):
     import subprocess
     out = subprocess.run(["ldd", so[0]], capture_output=True, text=True).stdout
     assert "oracle" not in out
+
+
+STRUCTS = {"pic_grid": "PicGrid", "pic_species": "PicSpecies",
+           "pic_species_adjoint": "PicSpeciesAdjoint", "pic_gr_metric": "PicGRMetric",
+           "pic_inject_params": "PicInjectParams", "pic_moment_params": "PicMomentParams",
+           "pic_field_bcs": "PicFieldBCs", "pic_gr_params": "PicGRParams",
+           "pic_step_params": "PicStepParams"}
+
+
+def test_binding_structs_match_header_layout(tmp_path):
+    """Every ctypes structure has the size and the field offsets the C
+    compiler gives the header's struct (gcc on this host)."""
+    import shutil
+    import subprocess
+    from entity_gb300 import abi
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "entity_pic.h"',
+             "int main(void) {"]
+    expect = []
+    for cname, pyname in STRUCTS.items():
+        cls = getattr(abi, pyname)
+        lines.append(f'  printf("%zu\\n", sizeof({cname}));')
+        expect.append(C.sizeof(cls))
+        for f in cls._fields_:
+            lines.append(f'  printf("%zu\\n", offsetof({cname}, {f[0]}));')
+            expect.append(getattr(cls, f[0]).offset)
+    lines.append("  return 0;\n}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.check_call(["gcc", "-std=c11", "-I", inc, str(src), "-o", str(exe)])
+    got = [int(x) for x in subprocess.check_output([str(exe)]).split()]
+    assert got == expect
