@@ -6,8 +6,10 @@
 // the call's particles (the largest current a particle can deposit into one
 // entry: the charge crossing a face within a step, or q w |v| for the
 // out-of-plane 2D component). The tiled kernel's exact per-tile integer sums
-// are scaled to this unit by a left shift, the per-particle kernel rounds its
-// contributions to the unit, and everything is added as 64-bit integers, so
+// are scaled to this unit by a left shift, the per-particle kernel rounds each
+// contribution to a multiple of 2^(ex - min(30, bits)) (a 32-bit conversion;
+// a 64-bit one runs on the FP64 pipe) and shifts it likewise, and everything
+// is added as 64-bit integers, so
 // the total of every entry is the same whatever the order of the additions.
 // A last pass converts each total to real_t once. With N particles in the
 // call, bits = min(34, 62 - ceil(log2(N + 1))) keeps every total below 2^62.

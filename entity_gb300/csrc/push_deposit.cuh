@@ -43,10 +43,17 @@ __global__ void __launch_bounds__(256) k_push_deposit(PDArgs<real> a) {
   float*        da[3]  = { a.sp.dx1, a.sp.dx2, a.sp.dx3 };
   float*        dpa[3] = { a.sp.dx1p, a.sp.dx2p, a.sp.dx3p };
   const int64_t n = a.list ? (int64_t)*a.list_count : a.sp.npart;
-  // scale of the exact accumulator: contributions in units of 2^(ex - bits)
+  // exact accumulator: each contribution is rounded to a multiple of
+  // 2^(ex - b) with b = min(30, bits), an int32 conversion (a 64-bit one
+  // runs on the FP64 pipe), then shifted to the call's unit 2^(ex - bits)
   float fj_scale = 0.f;
+  int   fj_shift = 0;
   if constexpr (sizeof(real) == 4 && MODE != MODE_PUSH) {
-    if (a.fj.p) fj_scale = ldexpf(1.f, a.fj.bits - a.fj.exponent());
+    if (a.fj.p) {
+      const int b = min(30, a.fj.bits);
+      fj_scale    = ldexpf(1.f, b - a.fj.exponent());
+      fj_shift    = a.fj.bits - b;
+    }
   }
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += stride) {
     const int64_t p = a.list ? (int64_t)a.list[t] : t;
@@ -128,8 +135,10 @@ __global__ void __launch_bounds__(256) k_push_deposit(PDArgs<real> a) {
         if (a.fj.p)
           ok = deposit_particle<D, O, real>(q, w[p], a.charge, a.inv_dt, a.dx, a.pc.ng, a.pc.ext,
                                             [&](int i, int j, int k, int c, real v) {
+                                              const int x = __float2int_rn(v * fj_scale);
                                               a.fj.add_units(i, j, k, c,
-                                                             __float2ll_rn(v * fj_scale));
+                                                             (long long)((unsigned long long)
+                                                                         (long long)x << fj_shift));
                                             });
         else
           ok = deposit_particle<D, O, real>(q, w[p], a.charge, a.inv_dt, a.dx, a.pc.ng, a.pc.ext,
