@@ -196,10 +196,35 @@ struct TiledGeom {
   static constexpr int    A          = 16 / (int)sizeof(real);
   static constexpr int    WEX_TMA    = ((WE0 + A - 1 + A - 1) / A) * A;
   static constexpr size_t kSmemMax   = 232448 - 128;  // per-CTA limit less the static words
-  static constexpr bool   TMA        = ((sizeof(real) * 6 * (size_t)WEX_TMA * WE1 * WE2 + 127) /
-                                        128) * 128 + jw_bytes <= kSmemMax;
+  static constexpr bool fits(int wx, int wy) {
+    return ((sizeof(real) * 6 * (size_t)wx * wy * WE2 + 127) / 128) * 128 + jw_bytes <= kSmemMax;
+  }
+  // The interpolation's lanes in one cell read x, x + 1, the next row and the
+  // next plane of a window row: the row and plane strides must differ in
+  // shared-memory bank (mod 32 words) or those reads conflict. The box's y
+  // extent is padded (rows beyond the window are loaded and never read)
+  // until x, x + 1, + row, + plane and their sums fall in 8 distinct banks.
+  static constexpr bool banks_distinct(int wx, int wy) {
+    // word offsets of the eight reads; a read of real_t covers w words
+    const int w = (int)sizeof(real) / 4, row = wx * w, pl = wx * wy * w;
+    const int o[8] = { 0, w, row, row + w, pl, pl + w, row + pl, row + pl + w };
+    for (int i = 0; i < 8; ++i)
+      for (int j = i + 1; j < 8; ++j) {
+        const int d = ((o[i] - o[j]) % 32 + 32) % 32;
+        if (d < w || d > 32 - w) return false;
+      }
+    return true;
+  }
+  static constexpr int pick_wey() {
+    int best = WE1;
+    for (int y = WE1 + 3; y >= WE1; --y)
+      if (D == 3 && banks_distinct(WEX_TMA, y) && fits(WEX_TMA, y)) best = y;
+    return best;
+  }
+  static constexpr bool   TMA        = fits(WEX_TMA, WE1);
   static constexpr int    WEX        = TMA ? WEX_TMA : WE0;
-  static constexpr int    NE         = WEX * WE1 * WE2;
+  static constexpr int    WEY        = TMA ? pick_wey() : WE1;
+  static constexpr int    NE         = WEX * WEY * WE2;
   static constexpr size_t eb_bytes   = sizeof(real) * 6 * (size_t)NE;
   static constexpr size_t smem_bytes = ((eb_bytes + 127) / 128) * 128 + jw_bytes;
 };
@@ -278,7 +303,7 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
           else inside = false;
         }
       }
-      EBs[R + wi + G::WEX * (wj + G::WE1 * (wk + G::WE2 * c))] =
+      EBs[R + wi + G::WEX * (wj + G::WEY * (wk + G::WE2 * c))] =
           inside ? a.EB.ld(gc[0] + ng, gc[1] + ng, D == 3 ? gc[2] + ng : 0, c) : (real)0;
     }
   }
@@ -327,7 +352,7 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT)
       return;
     }
   }
-  const SmemView<real> ebv{ EBs, g0[0] - R, g0[1], g0[2], G::WEX, G::WEX * G::WE1, G::NE };
+  const SmemView<real> ebv{ EBs, g0[0] - R, g0[1], g0[2], G::WEX, G::WEX * G::WEY, G::NE };
   const int joff[3] = { ng + T0[0] - H::J_LO, ng + T0[1] - H::J_LO,
                         D == 3 ? ng + T0[2] - H::J_LO : 0 };
 
