@@ -6,14 +6,31 @@
 
 namespace pic {
 
-__global__ void k_weight_bound(const float* w, int64_t n, float q, unsigned* bound) {
-  float m = 0.f;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
-       p += (int64_t)gridDim.x * blockDim.x)
-    m = fmaxf(m, fabsf(w[p]) * q);
+// max |w| |q| over the weights of up to kBoundSpecies species (blockIdx.y);
+// 16-byte loads where the array allows, one atomic per block
+__global__ void k_weight_bound(BoundArgs a) {
+  const int     s      = blockIdx.y;
+  const float*  w      = a.w[s];
+  const int64_t n      = a.n[s];
+  const int64_t tid    = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t n4     = (reinterpret_cast<uintptr_t>(w) % 16 == 0) ? n / 4 : 0;
+  const float4* w4     = reinterpret_cast<const float4*>(w);
+  float         m      = 0.f;
+  for (int64_t i = tid; i < n4; i += stride) {
+    const float4 v = w4[i];
+    m = fmaxf(m, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+  }
+  for (int64_t i = 4 * n4 + tid; i < n; i += stride) m = fmaxf(m, fabsf(w[i]));
+  // |q| max|w| = max |q||w|: multiplication by |q| >= 0 keeps the order
+  m = m * a.q[s];
   // non-negative floats order as their bit patterns
-  const unsigned b = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
-  if ((threadIdx.x & 31) == 0) atomicMax(bound, b);
+  __shared__ unsigned sm;
+  if (threadIdx.x == 0) sm = 0u;
+  __syncthreads();
+  atomicMax(&sm, __reduce_max_sync(0xffffffffu, __float_as_uint(m)));
+  __syncthreads();
+  if (threadIdx.x == 0) atomicMax(a.bound, sm);
 }
 
 // one block per row (j, k, c) of the grid at a time, threads along x
@@ -33,12 +50,15 @@ __global__ void k_fixed_to_real(FixedJ fj, FieldView<float> J, int e0, int e1, i
   }
 }
 
-cudaError_t launch_weight_bound(const float* w, int64_t n, float abs_charge, unsigned* bound,
-                                cudaStream_t s) {
-  if (n <= 0) return cudaSuccess;
-  int64_t blocks = (n + 255) / 256;
-  if (blocks > sm_count() * 16) blocks = sm_count() * 16;
-  PIC_KL(k_weight_bound<<<(unsigned)blocks, 256, 0, s>>>(w, n, abs_charge, bound));
+cudaError_t launch_weight_bound(const BoundArgs& a, cudaStream_t s) {
+  int64_t nmax = 0;
+  for (int k = 0; k < a.ns; ++k) nmax = a.n[k] > nmax ? a.n[k] : nmax;
+  if (a.ns <= 0 || nmax <= 0) return cudaSuccess;
+  // enough 256-thread blocks for one 16-byte load per thread, at most 4 per SM
+  int64_t blocks = (nmax / 4 + 255) / 256;
+  if (blocks > sm_count() * 4) blocks = sm_count() * 4;
+  if (blocks < 1) blocks = 1;
+  PIC_KL(k_weight_bound<<<dim3((unsigned)blocks, (unsigned)a.ns), 256, 0, s>>>(a));
   return cudaGetLastError();
 }
 

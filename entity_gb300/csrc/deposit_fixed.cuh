@@ -44,9 +44,17 @@ struct FixedJ {
   }
 };
 
-// bound = max(bound, max |w| |q|) over n weights
-cudaError_t launch_weight_bound(const float* w, int64_t n, float abs_charge, unsigned* bound,
-                                cudaStream_t s);
+// bound = max(bound, max |w| |q|) over the weights of up to kBoundSpecies
+// species in one launch
+constexpr int kBoundSpecies = 8;
+struct BoundArgs {
+  const float* w[kBoundSpecies];
+  int64_t      n[kBoundSpecies];
+  float        q[kBoundSpecies];  // |charge|
+  int          ns = 0;
+  unsigned*    bound = nullptr;
+};
+cudaError_t launch_weight_bound(const BoundArgs& a, cudaStream_t s);
 
 // J (+)= the totals in real_t: every element written when overwrite, else
 // the non-zero totals added; ext = the ghost-inclusive extents

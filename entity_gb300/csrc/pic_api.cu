@@ -584,15 +584,22 @@ bool arm_fixed_J(pic_ctx* c, const pic_species* sp, int32_t nspecies, double dt,
   if (cudaMemsetAsync(c->jfix, 0, sizeof(long long) * elems, s) != cudaSuccess ||
       cudaMemsetAsync(c->jfix_bound, 0, sizeof(unsigned), s) != cudaSuccess)
     return false;
-  int64_t ntot = 0;
+  int64_t         ntot = 0;
+  pic::BoundArgs  ba;
+  ba.bound = c->jfix_bound;
   for (int k = 0; k < nspecies; ++k) {
     const pic_species* q = sp + k;
     if (q->pusher == PIC_PUSHER_NONE || q->npart == 0 || q->charge == 0.0f) continue;
     ntot += q->npart;
-    if (pic::launch_weight_bound((const float*)q->weight, q->npart, std::fabs(q->charge),
-                                 c->jfix_bound, s) != cudaSuccess)
-      return false;
+    ba.w[ba.ns] = (const float*)q->weight;
+    ba.n[ba.ns] = q->npart;
+    ba.q[ba.ns] = std::fabs(q->charge);
+    if (++ba.ns == pic::kBoundSpecies) {
+      if (pic::launch_weight_bound(ba, s) != cudaSuccess) return false;
+      ba.ns = 0;
+    }
   }
+  if (ba.ns > 0 && pic::launch_weight_bound(ba, s) != cudaSuccess) return false;
   int lg = 0;
   while (lg < 62 && (int64_t(1) << lg) < ntot + 1) ++lg;
   fj->p         = c->jfix;
