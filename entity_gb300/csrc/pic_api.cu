@@ -905,8 +905,9 @@ int pic_sort(pic_ctx* c, pic_species* sp, uint32_t flags, int64_t* npart_out, vo
   add(sp->phi, (int)rb);
   for (int k = 0; k < sp->npld_r; ++k)
     add((char*)sp->pld_r + (size_t)k * sp->pld_r_stride[1] * rb, (int)rb, sp->pld_r_stride[0]);
+  // integer payloads are npart_t, 32-bit (global.h:385)
   for (int k = 0; k < sp->npld_i; ++k)
-    add((char*)sp->pld_i + (size_t)k * sp->pld_i_stride[1] * 8, 8, sp->pld_i_stride[0]);
+    add((char*)sp->pld_i + (size_t)k * sp->pld_i_stride[1] * 4, 4, sp->pld_i_stride[0]);
   // every array of a batch gets its own staging area when the context can
   // hold them (one gather, one copy back per batch); otherwise they go in
   // turn through one

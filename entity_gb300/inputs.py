@@ -82,7 +82,8 @@ class SpeciesArrays:
     npart: int = 0
     index: int = 1
     # optional: phi (real, 1D) and the payloads, 2D (particles x columns)
-    # tensors of real (pld_r) and int64 (pld_i) with any strides
+    # tensors of real (pld_r) and 32-bit integers (pld_i: the reference's
+    # npart_t is uint32) with any strides
     phi: torch.Tensor = None
     pld_r: torch.Tensor = None
     pld_i: torch.Tensor = None

@@ -87,6 +87,8 @@ def make_species(sp: SpeciesArrays, dim: int) -> abi.PicSpecies:
     for name in ("pld_r", "pld_i"):
         t = getattr(sp, name, None)
         if t is not None and t.numel() > 0:
+            if name == "pld_i" and t.element_size() != 4:
+                raise ValueError("pld_i holds 32-bit integers (npart_t)")
             setattr(ps, name, _ptr(t))
             st = getattr(ps, name + "_stride")
             st[0], st[1] = t.stride(0), t.stride(1)

@@ -102,7 +102,8 @@ typedef struct {
  * and the sort is asked to skip them. i3-arrays are unused in 2D.
  * The trailing fields are optional (zero them when unused): phi (real_t, the
  * reference keeps it for 2D non-Cartesian grids) and the payloads pld_r
- * (real_t) and pld_i (npart_t, 64-bit), npld_r / npld_i columns each, element
+ * (real_t) and pld_i (npart_t: 32-bit unsigned, global.h:385), npld_r /
+ * npld_i columns each, element
  * (p, k) at pld[p * pld_stride[0] + k * pld_stride[1]] (elements; a Kokkos
  * LayoutLeft View on the device has strides {1, maxnpart}). Only the sort and
  * dead removal touch them: particles carry their phi and payloads along. */

@@ -27,6 +27,10 @@ A second library per precision, oracle/_ref/libentity_ref_params_{f32,f64}.so,
 compiles oracle/ref_params.cpp with the reference's parameter sources
 (src/framework/parameters/*.cpp, src/global/utils/param_container.cpp,
 src/global/arch/kokkos_aliases.cpp) to run its own TOML-to-scales derivation.
+A third, oracle/_ref/libentity_ref_sort_{f32,f64}.so, compiles
+oracle/ref_sort.cpp with the reference's particle container and grid
+(src/framework/containers/particles.cpp, particles_sort.cpp,
+src/framework/domain/grid.cpp) to run its own RemoveDead and SortSpatially.
 
 The reference checkout is located by $ENTITY_REFERENCE, else
 /root/reference. Without it, build() returns {} and the tests that need these
@@ -95,6 +99,19 @@ def build(verbose=False, jobs=None):
         if _stale(target, deps + psrc[:1]):
             todo.append(["g++", *_flags(root), "-O1", *defs, *psrc, "-o", target])
 
+    # the reference's particle container and grid, for its own sort
+    # (Particles::RemoveDead and SortSpatially) driven by oracle/ref_sort.cpp
+    ssrc = [os.path.join(HERE, "ref_sort.cpp")]
+    ssrc += [os.path.join(root, "src", "framework", "containers", f)
+             for f in ("particles.cpp", "particles_sort.cpp")]
+    ssrc += [os.path.join(root, "src", "framework", "domain", "grid.cpp"),
+             os.path.join(root, "src", "global", "arch", "kokkos_aliases.cpp")]
+    for tag, defs in (("f32", ["-DSINGLE_PRECISION"]), ("f64", [])):
+        target = os.path.join(OUT, f"libentity_ref_sort_{tag}.so")
+        libs[("sort", tag)] = target
+        if _stale(target, deps + ssrc[:1]):
+            todo.append(["g++", *_flags(root), "-O1", *defs, *ssrc, "-o", target])
+
     def run(cmd):
         if verbose:
             print(" ".join(cmd), flush=True)
@@ -112,6 +129,17 @@ KERNEL_TESTS = ["deposit", "pusher", "gca_pusher", "ext_force", "prtl_bc", "fara
 # the reference's metric tests (tests/metrics/*.cpp): QKerrSchild against
 # Kerr-Schild at h = 0, 0.1 and 0.25, coordinate and vector transformations
 METRIC_TESTS = ["ks-qks", "ks-qks-4d", "coord_trans", "vec_trans"]
+# and its sort tests with the sources they link: the bin sort of a key
+# (tests/global/sorting.cpp), the tile index (tiling.cpp), and the particle
+# container's spatial sort (tests/framework/particles_sort.cpp)
+SORT_TESTS = {
+    "sorting": ("global", ["src/global/global.cpp"]),
+    "tiling": ("global", ["src/global/global.cpp"]),
+    "particles_sort": ("framework", ["src/global/global.cpp",
+                                     "src/framework/containers/particles.cpp",
+                                     "src/framework/containers/particles_sort.cpp",
+                                     "src/framework/domain/grid.cpp"]),
+}
 
 
 def build_tests(verbose=False, jobs=None):
@@ -126,15 +154,20 @@ def build_tests(verbose=False, jobs=None):
     deps = _deps(root)
     aliases = os.path.join(root, "src", "global", "arch", "kokkos_aliases.cpp")
     todo, exes = [], {}
-    for name in KERNEL_TESTS + METRIC_TESTS:
-        sub = "kernels" if name in KERNEL_TESTS else "metrics"
+    for name in KERNEL_TESTS + METRIC_TESTS + list(SORT_TESTS):
+        extra = []
+        if name in SORT_TESTS:
+            sub, rel = SORT_TESTS[name]
+            extra = [os.path.join(root, r) for r in rel]
+        else:
+            sub = "kernels" if name in KERNEL_TESTS else "metrics"
         src = os.path.join(root, "tests", sub, name + ".cpp")
         for tag, defs in (("f32", ["-DSINGLE_PRECISION"]), ("f64", [])):
             target = os.path.join(tdir, f"{name}_{tag}")
             exes[(name, tag)] = target
             if _stale(target, deps + [src]):
                 flags = [f for f in _flags(root) if f not in ("-shared", "-fPIC")]
-                todo.append(["g++", *flags, "-O1", *defs, src, aliases, "-o", target])
+                todo.append(["g++", *flags, "-O1", *defs, src, *extra, aliases, "-o", target])
 
     def run(cmd):
         if verbose:

@@ -29,6 +29,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <type_traits>
 #include <utility>
 #include <vector>
@@ -417,10 +418,60 @@ namespace Kokkos {
     deep_copy(dst, src);
   }
 
-  // subview: only the forms `subview(v, pair/ALL/index...)` keep a view of
-  // the same value type; ranges are [first, second)
+  // subview(v, a0, a1, ...): each argument is an index (the axis is
+  // dropped), a pair (the range [first, second)) or ALL; the result views the
+  // same memory with the parent's strides (the parent must outlive it)
   struct ALL_t {};
   inline constexpr ALL_t ALL {};
+
+  namespace shim {
+    template <class T, int R>
+    struct ptrs {
+      using type = typename ptrs<T, R - 1>::type*;
+    };
+    template <class T>
+    struct ptrs<T, 0> {
+      using type = T;
+    };
+    template <class A>
+    constexpr bool keeps_axis() {
+      return !std::is_integral_v<std::decay_t<A>>;
+    }
+    template <class A>
+    std::pair<std::size_t, std::size_t> sub_range(const A& a, std::size_t n) {
+      if constexpr (std::is_same_v<std::decay_t<A>, ALL_t>) {
+        return { 0, n };
+      } else if constexpr (std::is_integral_v<std::decay_t<A>>) {
+        return { static_cast<std::size_t>(a), 1 };
+      } else {
+        return { static_cast<std::size_t>(a.first),
+                 static_cast<std::size_t>(a.second) - static_cast<std::size_t>(a.first) };
+      }
+    }
+  } // namespace shim
+
+  template <class DT, class... P, class... Args>
+  auto subview(const View<DT, P...>& v, const Args&... args) {
+    using V = View<DT, P...>;
+    static_assert(sizeof...(Args) == V::rank, "subview: one argument per axis");
+    constexpr int R = (0 + ... + int(shim::keeps_axis<Args>()));
+    using Out       = View<typename shim::ptrs<typename V::value_type, R>::type, HostSpace>;
+    std::size_t off = 0, ext[8] = {}, str[8] = {};
+    int         r = 0, d = 0;
+    (
+      [&] {
+        const auto rg = shim::sub_range(args, v.extent(d));
+        off += rg.first * v.stride(d);
+        if (shim::keeps_axis<Args>()) {
+          ext[r] = rg.second;
+          str[r] = v.stride(d);
+          ++r;
+        }
+        ++d;
+      }(),
+      ...);
+    return Out::wrap_strided(v.data() + off, ext, str);
+  }
 
   // ------------------------------------------------------------ policies
   template <unsigned N>
@@ -511,12 +562,17 @@ namespace Kokkos {
     // RangePolicy or an MDRangePolicy) in LayoutRight order, the last index
     // fastest; with ENTITY_SHIM_OPENMP and `par` the outermost loop is split
     // statically over the threads
+    // true: every parallel_for runs serially in index order, so that kernels
+    // that hand out slots with atomics (stream compaction) give the order a
+    // serial host gives (set around calls whose output order is compared)
+    inline bool g_serial = false;
+
     template <bool par, class Policy, class V>
     inline void iterate(const Policy& pol, const V& v) {
       if constexpr (std::is_integral_v<Policy>) {
         const std::int64_t n = static_cast<std::int64_t>(pol);
 #if defined(ENTITY_SHIM_OPENMP)
-#pragma omp parallel for schedule(static) if (par)
+#pragma omp parallel for schedule(static) if (par && !g_serial)
 #endif
         for (std::int64_t i = 0; i < n; ++i) {
           v(i);
@@ -526,7 +582,7 @@ namespace Kokkos {
         const auto&        lo = pol.lo;
         const auto&        hi = pol.hi;
 #if defined(ENTITY_SHIM_OPENMP)
-#pragma omp parallel for schedule(static) if (par)
+#pragma omp parallel for schedule(static) if (par && !g_serial)
 #endif
         for (std::int64_t i0 = lo[0]; i0 < hi[0]; ++i0) {
           if constexpr (N == 1) {
@@ -551,7 +607,7 @@ namespace Kokkos {
         }
       } else {
 #if defined(ENTITY_SHIM_OPENMP)
-#pragma omp parallel for schedule(static) if (par)
+#pragma omp parallel for schedule(static) if (par && !g_serial)
 #endif
         for (std::int64_t i = pol.begin(); i < pol.end(); ++i) {
           v(i);
@@ -656,6 +712,17 @@ namespace Kokkos {
   inline void parallel_reduce(const std::string&, const Policy& pol, const F& f, R&& result) {
     parallel_reduce(pol, f, std::forward<R>(result));
   }
+  // several plain scalars reduced by sum in one pass (serial, in index order)
+  template <class Policy, class F, class R1, class R2, class... Rs>
+  inline void parallel_reduce(const std::string&, const Policy& pol, const F& f, R1& r1, R2& r2,
+                              Rs&... rs) {
+    using Tag = typename shim::tag_of<Policy>::type;
+    std::tuple<R1, R2, Rs...> acc {};
+    shim::iterate<false>(pol, [&](auto... i) {
+      std::apply([&](auto&... a) { shim::invoke<Tag>(f, i..., a...); }, acc);
+    });
+    std::tie(r1, r2, rs...) = acc;
+  }
 
   // ------------------------------------------------------------ random
   // Only the types appear on the hot path (initial conditions come from the
@@ -673,6 +740,9 @@ namespace Kokkos {
       return m_s * 2685821657736338717ull;
     }
     std::uint32_t urand() { return static_cast<std::uint32_t>(urand64() >> 32); }
+    // uniform in [0, range) and [lo, hi)
+    std::uint32_t urand(std::uint32_t range) { return range ? urand() % range : 0u; }
+    std::uint32_t urand(std::uint32_t lo, std::uint32_t hi) { return lo + urand(hi - lo); }
     float  frand() { return static_cast<float>(urand64() >> 40) * (1.0f / 16777216.0f); }
     double drand() { return static_cast<double>(urand64() >> 11) * (1.0 / 9007199254740992.0); }
     float  frand(float r) { return frand() * r; }

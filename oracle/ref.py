@@ -68,6 +68,20 @@ def lib(real, order):
     return _libs[key]
 
 
+def sort_lib(real):
+    key = ("sort", "f32" if real == torch.float32 else "f64")
+    if key not in _libs:
+        paths = build_ref.build()
+        if key not in paths:
+            raise RuntimeError("the reference checkout is not available")
+        L = C.CDLL(paths[key])
+        L.ref_sort.restype = C.c_int64
+        L.ref_sort.argtypes = [C.POINTER(OrcGrid), C.POINTER(OrcSpecies), C.c_int, C.c_void_p,
+                               C.c_int, C.c_void_p, C.c_int]
+        _libs[key] = L
+    return _libs[key]
+
+
 def _check(rc):
     if rc != 0:
         raise RuntimeError(f"reference kernel call failed ({rc})")
@@ -109,6 +123,25 @@ class RefOracle(Oracle):
     def gr_filter_pass(self, J, buff, axis_min=1, axis_max=1):
         _check(self.R.ref_filter_pass_axisym(C.byref(self.og), _p(J), _p(buff), axis_min,
                                              axis_max))
+
+    def sort_particles(self, sp, remove_dead, pld_r=None, pld_i=None):
+        """Particles::RemoveDead (when remove_dead) and SortSpatially of the
+        reference's own particle container on the species, in place; the
+        payloads (row-major particle x column tensors, pld_i int32) move with
+        it. Returns the new particle count."""
+        S = sort_lib(self.g.real)
+        s = self.species(sp)
+        nr = 0 if pld_r is None else pld_r.shape[1]
+        ni = 0 if pld_i is None else pld_i.shape[1]
+        assert pld_r is None or pld_r.is_contiguous()
+        assert pld_i is None or (pld_i.is_contiguous() and pld_i.dtype == torch.int32)
+        n = S.ref_sort(C.byref(self.og), C.byref(s), int(remove_dead),
+                       None if pld_r is None else _p(pld_r), nr,
+                       None if pld_i is None else _p(pld_i), ni)
+        if n < 0:
+            raise RuntimeError("reference sort failed")
+        sp.npart = int(n)
+        return int(n)
 
     def sort_keys(self, sp):
         s = self.species(sp)

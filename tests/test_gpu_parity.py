@@ -305,8 +305,9 @@ def test_sort_carries_phi_and_payloads(flags, real):
     sp.tag[torch.rand(n, generator=gen) < 0.1] = 0
     sp.phi = torch.rand(n, generator=gen, dtype=torch.float64).to(real)
     sp.pld_r = torch.rand(3, n, generator=gen, dtype=torch.float64).to(real).t()  # strides (1, n)
-    sp.pld_i = torch.stack([torch.arange(n, dtype=torch.int64),
-                            torch.randint(0, 1 << 40, (n,), generator=gen)], dim=1)
+    sp.pld_i = torch.stack([torch.arange(n, dtype=torch.int32),
+                            torch.randint(-(1 << 31), 1 << 31, (n,), generator=gen,
+                                          dtype=torch.int32)], dim=1)
     assert sp.pld_r.stride() == (1, n) and sp.pld_i.stride() == (2, 1)
     ref = sp.clone()
     spg = sp.clone().to("cuda")
@@ -315,7 +316,7 @@ def test_sort_carries_phi_and_payloads(flags, real):
     assert ctx.sort(spg, flags) == abi.PIC_OK
     torch.cuda.synchronize()
     m = spg.npart
-    orig = spg.pld_i[:m, 0].cpu()
+    orig = spg.pld_i[:m, 0].cpu().long()
     # a permutation of the original particles (the alive ones after removal)
     assert torch.equal(orig.sort().values,
                        (torch.nonzero(ref.tag == 1).flatten() if flags & abi.PIC_SORT_REMOVE_DEAD

@@ -65,7 +65,8 @@ def _assert_species_equal(a, b, dim):
 
 
 @pytest.mark.parametrize("tag", ["f32", "f64"])
-@pytest.mark.parametrize("name", build_ref.KERNEL_TESTS + build_ref.METRIC_TESTS)
+@pytest.mark.parametrize("name", build_ref.KERNEL_TESTS + build_ref.METRIC_TESTS +
+                         list(build_ref.SORT_TESTS))
 def test_reference_kernel_tests_pass_on_the_shim(name, tag, tmp_path):
     exe = build_ref.build_tests()[(name, tag)]
     # some write logs into their working directory
@@ -189,6 +190,62 @@ def test_3d_filter_quirk_is_the_references():
     c = J[0, ng + 3:ng + 6, ng + 3:ng + 6, ng + 3:ng + 6]   # (k, j, i)
     assert float(c[0, 1, 1]) == pytest.approx(3 / 32) and float(c[2, 1, 1]) == pytest.approx(3 / 32)
     assert float(c[0, 2, 1]) == 0.0 and float(c[2, 0, 1]) == 0.0
+
+
+@pytest.mark.parametrize("remove_dead", [False, True])
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("dim", [2, 3])
+def test_sort_matches_reference_container(dim, real, remove_dead):
+    # Particles::RemoveDead + Particles::SortSpatially of the reference's own
+    # container (particles_sort.cpp:103-253, run serially: the alive slots and
+    # the bins fill in the particles' order) against the oracle's dead removal
+    # and stable cell-key sort: every array equal, the count too
+    g = _grid(dim, 1, real)
+    sp = make_species(g, 5, 0.1, 0.0, 8)
+    gen = torch.Generator().manual_seed(12)
+    perm = torch.randperm(sp.npart, generator=gen)
+    for lst in (sp.i, sp.dx, sp.i_prev, sp.dx_prev, sp.u):
+        for d in range(len(lst)):
+            lst[d] = lst[d][perm].contiguous()
+    sp.w, sp.tag = sp.w[perm].contiguous(), sp.tag[perm].contiguous()
+    sp.tag[torch.rand(sp.npart, generator=gen) < 0.15] = 0
+    a, b = sp.clone(), sp.clone()
+    n = _ref(g).sort_particles(a, remove_dead)
+    o = Oracle(g)
+    if remove_dead:
+        o.remove_dead(b)
+    o.sort(b)
+    assert n == b.npart == (int((sp.tag == 1).sum()) if remove_dead else sp.npart)
+    cut = lambda x: x[:n]
+    for d in range(dim):
+        for name, xa, xb in (("i", a.i, b.i), ("dx", a.dx, b.dx), ("i_prev", a.i_prev, b.i_prev),
+                             ("dx_prev", a.dx_prev, b.dx_prev)):
+            assert torch.equal(cut(xa[d]), cut(xb[d])), f"{name}{d + 1}"
+    for d in range(3):
+        assert torch.equal(cut(a.u[d]), cut(b.u[d])), f"u{d + 1}"
+    assert torch.equal(cut(a.w), cut(b.w)) and torch.equal(cut(a.tag), cut(b.tag))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_reference_sort_moves_payloads(dim):
+    # the reference's container carries every payload column with its
+    # particle (particles_sort.cpp:169-177, 245-251); pld_i[:, 0] holds each
+    # particle's original index, pld_i is npart_t (32-bit)
+    g = _grid(dim, 1, torch.float64)
+    sp = make_species(g, 4, 0.1, 0.0, 9)
+    sp.tag[::5] = 0
+    n0 = sp.npart
+    gen = torch.Generator().manual_seed(4)
+    pld_r = torch.rand(n0, 3, generator=gen, dtype=torch.float64)
+    pld_i = torch.stack([torch.arange(n0, dtype=torch.int32),
+                         torch.randint(0, 1 << 30, (n0,), generator=gen, dtype=torch.int32)], 1)
+    ref_i, ref_r, ref_u = pld_i.clone(), pld_r.clone(), sp.u[0].clone()
+    a = sp.clone()
+    n = _ref(g).sort_particles(a, True, pld_r, pld_i)
+    orig = pld_i[:n, 0].long()
+    assert torch.equal(orig.sort().values, torch.nonzero(sp.tag == 1).flatten())
+    assert torch.equal(pld_r[:n], ref_r[orig]) and torch.equal(pld_i[:n], ref_i[orig])
+    assert torch.equal(a.u[0][:n], ref_u[orig])
 
 
 @pytest.mark.parametrize("dim", [2, 3])
