@@ -3,7 +3,7 @@ reference sources against the host Kokkos shim (TEST INFRASTRUCTURE ONLY).
 
 RefOracle has the Oracle's interface for the kernels the reference build
 provides (push, deposit, Faraday, Ampere, CurrentsAmpere, one filter pass,
-the sort key) and keeps the restated exchange routines for the rest, so
+the field exchange through comm::CommunicateField, the sort key), so
 Oracle.step runs the reference's kernels in the reference's step order.
 """
 import ctypes as C
@@ -64,6 +64,8 @@ def lib(real, order):
         L.ref_gr_deposit.argtypes = [G, PD, S, V, D]
         L.ref_sort_keys.restype = C.c_int
         L.ref_sort_keys.argtypes = [G, S, C.POINTER(C.c_uint32)]
+        L.ref_communicate.argtypes = [G, V, C.c_int, C.c_int, C.c_int]
+        L.ref_sync_currents.argtypes = [G, V, V]
         _libs[key] = L
     return _libs[key]
 
@@ -123,6 +125,12 @@ class RefOracle(Oracle):
     def gr_filter_pass(self, J, buff, axis_min=1, axis_max=1):
         _check(self.R.ref_filter_pass_axisym(C.byref(self.og), _p(J), _p(buff), axis_min,
                                              axis_max))
+
+    def fill_ghosts(self, fld, is_em, c0, c1):
+        _check(self.R.ref_communicate(C.byref(self.og), _p(fld), int(is_em), c0, c1))
+
+    def sync_currents(self, J, buff):
+        _check(self.R.ref_sync_currents(C.byref(self.og), _p(J), _p(buff)))
 
     def sort_particles(self, sp, remove_dead, pld_r=None, pld_i=None):
         """Particles::RemoveDead (when remove_dead) and SortSpatially of the

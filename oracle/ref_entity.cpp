@@ -13,7 +13,9 @@
 #include "enums.h"
 #include "global.h"
 
+#include "arch/directions.h"
 #include "arch/kokkos_aliases.h"
+#include "framework/domain/comm_nompi.hpp"
 #include "metrics/minkowski.h"
 #include "metrics/qkerr_schild.h"
 #include "utils/sorting.h"
@@ -295,6 +297,82 @@ namespace {
                          f);
   }
 
+  // ---- field exchange of one periodic domain -----------------------------
+  // Metadomain::CommunicateFields / SynchronizeFields (metadomain_comm.cpp:
+  // 204-367, 408-562) for a domain that is its own neighbour along every
+  // periodic axis: the send and receive slices of GetSendRecvParams
+  // (metadomain_comm.cpp:117-193) around the reference's
+  // comm::CommunicateField (comm_nompi.hpp), over dir::Directions<D>::all. A
+  // direction with a component along a non-periodic axis has no neighbour
+  // and is skipped, as GetSendRecvRanks leaves it.
+  template <Dimension D>
+  bool exchange_slices(const orc_grid* g, const dir::direction_t<D>& dir, bool synchronize,
+                       std::vector<cell_range_t>& send, std::vector<cell_range_t>& recv) {
+    const int n[3] = { g->n1, g->n2, g->n3 };
+    for (auto d { 0u }; d < dir.size(); ++d) {
+      if (dir[d] != 0 && !g->periodic[d]) {
+        return false;
+      }
+    }
+    for (auto d { 0u }; d < dir.size(); ++d) {
+      const ncells_t imin = N_GHOSTS, imax = N_GHOSTS + (ncells_t)n[d];
+      const int      dr = dir[d];
+      if (!synchronize) {
+        // send from the active zones, receive into the ghost zones
+        send.emplace_back(dr == 0 ? imin : (dr == 1 ? imax - N_GHOSTS : imin),
+                          dr == 0 ? imax : (dr == 1 ? imax : imin + N_GHOSTS));
+        recv.emplace_back(-dr == 0 ? imin : (-dr == 1 ? imax : imin - N_GHOSTS),
+                          -dr == 0 ? imax : (-dr == 1 ? imax + N_GHOSTS : imin));
+      } else {
+        // send from and receive into active + ghost zones
+        send.emplace_back(dr == 0 ? imin - N_GHOSTS : (dr == 1 ? imax - N_GHOSTS : imin - N_GHOSTS),
+                          dr == 0 ? imax + N_GHOSTS : (dr == 1 ? imax + N_GHOSTS : imin + N_GHOSTS));
+        recv.emplace_back(-dr == 0 ? imin - N_GHOSTS : (-dr == 1 ? imax - N_GHOSTS : imin - N_GHOSTS),
+                          -dr == 0 ? imax + N_GHOSTS : (-dr == 1 ? imax + N_GHOSTS : imin + N_GHOSTS));
+      }
+    }
+    return true;
+  }
+
+  template <Dimension D, unsigned short N>
+  void communicate(const orc_grid* g, void* fld, const int64_t* s, int c0, int c1) {
+    auto f = wrap_field<D, N>(g, fld, s);
+    for (const auto& dir : dir::Directions<D>::all) {
+      std::vector<cell_range_t> send, recv;
+      if (!exchange_slices<D>(g, dir, false, send, recv)) {
+        continue;
+      }
+      comm::CommunicateField<D, N>(0, f, f, 0, 0, 0, 0, send, recv,
+                                   cell_range_t((ncells_t)c0, (ncells_t)c1), false);
+    }
+  }
+
+  template <Dimension D>
+  void synchronize_currents(const orc_grid* g, void* J, void* buff) {
+    auto cur = wrap_field<D, 3>(g, J, g->cur_s);
+    auto bf  = wrap_field<D, 3>(g, buff, g->cur_s);
+    Kokkos::deep_copy(bf, ZERO);
+    for (const auto& dir : dir::Directions<D>::all) {
+      std::vector<cell_range_t> send, recv;
+      if (!exchange_slices<D>(g, dir, true, send, recv)) {
+        continue;
+      }
+      comm::CommunicateField<D, 3>(0, cur, bf, 0, 0, 0, 0, send, recv, cell_range_t(0, 3), true);
+    }
+    // AddBufferedFields over the active cells (metadomain_comm.cpp:370-406)
+    const std::size_t ng = N_GHOSTS;
+    if constexpr (D == Dim::_2D) {
+      for (std::size_t i = ng; i < ng + (std::size_t)g->n1; ++i)
+        for (std::size_t j = ng; j < ng + (std::size_t)g->n2; ++j)
+          for (int c = 0; c < 3; ++c) cur(i, j, c) += bf(i, j, c);
+    } else {
+      for (std::size_t i = ng; i < ng + (std::size_t)g->n1; ++i)
+        for (std::size_t j = ng; j < ng + (std::size_t)g->n2; ++j)
+          for (std::size_t k = ng; k < ng + (std::size_t)g->n3; ++k)
+            for (int c = 0; c < 3; ++c) cur(i, j, k, c) += bf(i, j, k, c);
+    }
+  }
+
   // ---- GR: metric::QKerrSchild<Dim::_2D> --------------------------------
   // mp = { x1min, x1max, x2min, x2max, a, r0, h }
   using QKS = metric::QKerrSchild<Dim::_2D>;
@@ -517,6 +595,28 @@ int ref_currents_ampere(const orc_grid* g, void* EB, void* J, double coeff, doub
     g,
     [&] { currents_ampere<Dim::_2D>(g, EB, J, coeff, ppc0); },
     [&] { currents_ampere<Dim::_3D>(g, EB, J, coeff, ppc0); });
+}
+
+// CommunicateFields on a field of the em (is_em) or cur layout, components
+// [c0, c1): the ghost zones refilled from the active zones
+int ref_communicate(const orc_grid* g, void* fld, int is_em, int c0, int c1) {
+  return dispatch(
+    g,
+    [&] {
+      if (is_em) communicate<Dim::_2D, 6>(g, fld, g->em_s, c0, c1);
+      else       communicate<Dim::_2D, 3>(g, fld, g->cur_s, c0, c1);
+    },
+    [&] {
+      if (is_em) communicate<Dim::_3D, 6>(g, fld, g->em_s, c0, c1);
+      else       communicate<Dim::_3D, 3>(g, fld, g->cur_s, c0, c1);
+    });
+}
+
+// SynchronizeFields(J): the additive fold of J's ghost and edge zones
+int ref_sync_currents(const orc_grid* g, void* J, void* buff) {
+  return dispatch(
+    g, [&] { synchronize_currents<Dim::_2D>(g, J, buff); },
+    [&] { synchronize_currents<Dim::_3D>(g, J, buff); });
 }
 
 int ref_filter_pass(const orc_grid* g, void* J, void* buff) {

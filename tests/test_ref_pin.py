@@ -192,6 +192,28 @@ def test_3d_filter_quirk_is_the_references():
     assert float(c[0, 2, 1]) == 0.0 and float(c[2, 0, 1]) == 0.0
 
 
+@pytest.mark.parametrize("periodic", [(1, 1, 1), (0, 1, 1), (1, 0, 0)])
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("dim", [2, 3])
+def test_field_exchange_matches_reference(dim, real, periodic):
+    # Metadomain::SynchronizeFields(J) and CommunicateFields for one domain
+    # that is its own neighbour along its periodic axes, through the
+    # reference's comm::CommunicateField over Directions<D>::all
+    g = _grid(dim, 2, real, periodic=periodic)
+    o, r = Oracle(g), _ref(g)
+    Ja = random_currents(g, 31)
+    Jb = Ja.clone()
+    o.sync_currents(Ja, empty_field(g, 3))
+    r.sync_currents(Jb, empty_field(g, 3))
+    assert torch.equal(Ja, Jb)
+    for is_em, c0, c1 in ((False, 0, 3), (True, 0, 6), (True, 0, 3), (True, 3, 6)):
+        Fa = random_fields(g, 32) if is_em else random_currents(g, 33)
+        Fb = Fa.clone()
+        o.fill_ghosts(Fa, is_em, c0, c1)
+        r.fill_ghosts(Fb, is_em, c0, c1)
+        assert torch.equal(Fa, Fb), (is_em, c0, c1)
+
+
 @pytest.mark.parametrize("remove_dead", [False, True])
 @pytest.mark.parametrize("real", REALS)
 @pytest.mark.parametrize("dim", [2, 3])
