@@ -129,22 +129,29 @@ KERNEL_TESTS = ["deposit", "pusher", "gca_pusher", "ext_force", "prtl_bc", "fara
 # the reference's metric tests (tests/metrics/*.cpp): QKerrSchild against
 # Kerr-Schild at h = 0, 0.1 and 0.25, coordinate and vector transformations
 METRIC_TESTS = ["ks-qks", "ks-qks-4d", "coord_trans", "vec_trans"]
-# and its sort tests with the sources they link: the bin sort of a key
-# (tests/global/sorting.cpp), the tile index (tiling.cpp), and the particle
-# container's spatial sort (tests/framework/particles_sort.cpp)
-SORT_TESTS = {
+# and its framework tests with the sources they link: the bin sort of a key
+# (tests/global/sorting.cpp), the tile index (tiling.cpp), the particle
+# container and its spatial sort (tests/framework/particles.cpp,
+# particles_sort.cpp), the field container (fields.cpp) and the single-domain
+# field exchange (comm-nompi.cpp)
+LINKED_TESTS = {
     "sorting": ("global", ["src/global/global.cpp"]),
     "tiling": ("global", ["src/global/global.cpp"]),
+    "particles": ("framework", ["src/global/global.cpp",
+                                "src/framework/containers/particles.cpp"]),
     "particles_sort": ("framework", ["src/global/global.cpp",
                                      "src/framework/containers/particles.cpp",
                                      "src/framework/containers/particles_sort.cpp",
                                      "src/framework/domain/grid.cpp"]),
+    "fields": ("framework", ["src/global/global.cpp",
+                             "src/framework/containers/fields.cpp"]),
+    "comm-nompi": ("framework", ["src/global/global.cpp"]),
 }
 
 
 def build_tests(verbose=False, jobs=None):
-    """Compiles the reference's kernel and metric tests unmodified against
-    the shim into oracle/_ref/tests/<name>_{f32,f64}; returns
+    """Compiles the reference's kernel, metric and framework tests unmodified
+    against the shim into oracle/_ref/tests/<name>_{f32,f64}; returns
     {(name, tag): path}."""
     root = reference_root()
     if root is None:
@@ -154,10 +161,10 @@ def build_tests(verbose=False, jobs=None):
     deps = _deps(root)
     aliases = os.path.join(root, "src", "global", "arch", "kokkos_aliases.cpp")
     todo, exes = [], {}
-    for name in KERNEL_TESTS + METRIC_TESTS + list(SORT_TESTS):
+    for name in KERNEL_TESTS + METRIC_TESTS + list(LINKED_TESTS):
         extra = []
-        if name in SORT_TESTS:
-            sub, rel = SORT_TESTS[name]
+        if name in LINKED_TESTS:
+            sub, rel = LINKED_TESTS[name]
             extra = [os.path.join(root, r) for r in rel]
         else:
             sub = "kernels" if name in KERNEL_TESTS else "metrics"

@@ -66,7 +66,7 @@ def _assert_species_equal(a, b, dim):
 
 @pytest.mark.parametrize("tag", ["f32", "f64"])
 @pytest.mark.parametrize("name", build_ref.KERNEL_TESTS + build_ref.METRIC_TESTS +
-                         list(build_ref.SORT_TESTS))
+                         list(build_ref.LINKED_TESTS))
 def test_reference_kernel_tests_pass_on_the_shim(name, tag, tmp_path):
     exe = build_ref.build_tests()[(name, tag)]
     # some write logs into their working directory
