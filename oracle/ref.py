@@ -66,6 +66,7 @@ def lib(real, order):
         L.ref_sort_keys.argtypes = [G, S, C.POINTER(C.c_uint32)]
         L.ref_communicate.argtypes = [G, V, C.c_int, C.c_int, C.c_int]
         L.ref_sync_currents.argtypes = [G, V, V]
+        L.ref_conductor_walls.argtypes = [G, V, C.c_int, C.c_int]
         _libs[key] = L
     return _libs[key]
 
@@ -125,6 +126,10 @@ class RefOracle(Oracle):
     def gr_filter_pass(self, J, buff, axis_min=1, axis_max=1):
         _check(self.R.ref_filter_pass_axisym(C.byref(self.og), _p(J), _p(buff), axis_min,
                                              axis_max))
+
+    def conductor_walls(self, EB, set_e, set_b):
+        """The CONDUCTOR sides of the grid's field boundaries (set_field_bcs)."""
+        _check(self.R.ref_conductor_walls(C.byref(self.og), _p(EB), int(set_e), int(set_b)))
 
     def fill_ghosts(self, fld, is_em, c0, c1):
         _check(self.R.ref_communicate(C.byref(self.og), _p(fld), int(is_em), c0, c1))

@@ -373,6 +373,53 @@ namespace {
     }
   }
 
+  // ---- SR perfect-conductor walls ----------------------------------------
+  // srpic::FieldBoundaries (srpic/fields_bcs.h:622-672) for the CONDUCTOR
+  // sides, in Directions<D>::orth order: PerfectConductorFieldsIn's range
+  // (fields_bcs.h:356-396: the ghost layers and the edge, N_GHOSTS + 1 cells
+  // on the lower side) and ConductorBoundaries_kernel (fields_bcs.hpp:523-800)
+  template <Dimension D, in O, bool P>
+  void conductor_side(const orc_grid* g, ndfield_t<D, 6>& em, ncells_t i_edge, BCTags tags,
+                      const std::int64_t* lo, const std::int64_t* hi) {
+    if constexpr (D == Dim::_2D) {
+      Kokkos::parallel_for(Kokkos::MDRangePolicy<Kokkos::Rank<2>>({ lo[0], lo[1] }, { hi[0], hi[1] }),
+                           kernel::bc::ConductorBoundaries_kernel<D, O, P>(em, i_edge, tags));
+    } else {
+      Kokkos::parallel_for(
+        Kokkos::MDRangePolicy<Kokkos::Rank<3>>({ lo[0], lo[1], lo[2] }, { hi[0], hi[1], hi[2] }),
+        kernel::bc::ConductorBoundaries_kernel<D, O, P>(em, i_edge, tags));
+    }
+  }
+
+  template <Dimension D>
+  void conductor_walls(const orc_grid* g, void* EB, int set_e, int set_b) {
+    auto         em   = wrap_field<D, 6>(g, EB, g->em_s);
+    const BCTags tags = (set_e ? (BCTags)BC::E : (BCTags)0) | (set_b ? (BCTags)BC::B : (BCTags)0);
+    const int    n[3] = { g->n1, g->n2, g->n3 };
+    for (const auto& dir : dir::Directions<D>::orth) {
+      const auto sign = dir.get_sign();
+      const int  d    = (int)dir.get_dim();
+      if (g->fbc[d][sign > 0 ? 1 : 0] != 2) {
+        continue;
+      }
+      std::int64_t lo[3] = { 0, 0, 0 }, hi[3] = { 0, 0, 0 };
+      for (int a = 0; a < (int)D; ++a) {
+        hi[a] = (a == d) ? (sign < 0 ? N_GHOSTS + 1 : N_GHOSTS) : n[a] + 2 * N_GHOSTS;
+      }
+      const ncells_t i_edge = sign > 0 ? N_GHOSTS + (ncells_t)n[d] : N_GHOSTS;
+      if (d == 0) {
+        if (sign > 0) conductor_side<D, in::x1, true>(g, em, i_edge, tags, lo, hi);
+        else          conductor_side<D, in::x1, false>(g, em, i_edge, tags, lo, hi);
+      } else if (d == 1) {
+        if (sign > 0) conductor_side<D, in::x2, true>(g, em, i_edge, tags, lo, hi);
+        else          conductor_side<D, in::x2, false>(g, em, i_edge, tags, lo, hi);
+      } else if constexpr (D == Dim::_3D) {
+        if (sign > 0) conductor_side<D, in::x3, true>(g, em, i_edge, tags, lo, hi);
+        else          conductor_side<D, in::x3, false>(g, em, i_edge, tags, lo, hi);
+      }
+    }
+  }
+
   // ---- GR: metric::QKerrSchild<Dim::_2D> --------------------------------
   // mp = { x1min, x1max, x2min, x2max, a, r0, h }
   using QKS = metric::QKerrSchild<Dim::_2D>;
@@ -610,6 +657,13 @@ int ref_communicate(const orc_grid* g, void* fld, int is_em, int c0, int c1) {
       if (is_em) communicate<Dim::_3D, 6>(g, fld, g->em_s, c0, c1);
       else       communicate<Dim::_3D, 3>(g, fld, g->cur_s, c0, c1);
     });
+}
+
+// the perfect-conductor sides of g->fbc (2) on EB
+int ref_conductor_walls(const orc_grid* g, void* EB, int set_e, int set_b) {
+  return dispatch(
+    g, [&] { conductor_walls<Dim::_2D>(g, EB, set_e, set_b); },
+    [&] { conductor_walls<Dim::_3D>(g, EB, set_e, set_b); });
 }
 
 // SynchronizeFields(J): the additive fold of J's ghost and edge zones

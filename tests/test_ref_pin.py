@@ -214,6 +214,27 @@ def test_field_exchange_matches_reference(dim, real, periodic):
         assert torch.equal(Fa, Fb), (is_em, c0, c1)
 
 
+@pytest.mark.parametrize("sides", ["x1", "x2", "all"])
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("dim", [2, 3])
+def test_conductor_walls_match_reference(dim, real, sides):
+    # srpic::FieldBoundaries for CONDUCTOR sides: PerfectConductorFieldsIn's
+    # ranges and ConductorBoundaries_kernel, in Directions<D>::orth order
+    kinds = {"x1": [(2, 2), (0, 0), (0, 0)], "x2": [(0, 0), (2, 2), (0, 0)],
+             "all": [(2, 2), (2, 2), (2, 2)]}[sides][:dim]
+    periodic = tuple(int(k[0] == 0) for k in kinds) + (1,) * (3 - dim)
+    g = _grid(dim, 2, real, periodic=periodic)
+    o, r = Oracle(g), _ref(g)
+    for x in (o, r):
+        x.set_field_bcs(kinds)
+    for set_e, set_b in ((1, 0), (0, 1), (1, 1)):
+        Fa = random_fields(g, 40 + set_e + 2 * set_b)
+        Fb = Fa.clone()
+        o.field_boundaries(Fa, set_e, set_b)
+        r.conductor_walls(Fb, set_e, set_b)
+        assert torch.equal(Fa, Fb), (set_e, set_b)
+
+
 @pytest.mark.parametrize("remove_dead", [False, True])
 @pytest.mark.parametrize("real", REALS)
 @pytest.mark.parametrize("dim", [2, 3])
