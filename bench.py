@@ -218,7 +218,7 @@ def cpu_sample(w, steps, warmup=1, n=None, sort_interval=0, target_s=10.0):
     the workload with the same per-cell content; with sort_interval > 0 it
     sorts by the reference's cell key as often as the GPU arm sorts.
     steps=None times as many steps as fill about target_s seconds, judged
-    from the warm-up steps (2 to 200)."""
+    from the warm-up steps (at least 10, at most 200)."""
     from oracle.oracle import Oracle, lib
     n = n or w["sample_n"]
     g, EB, J, buff, sp = make_setup(w, "cpu", n=n)
@@ -236,7 +236,7 @@ def cpu_sample(w, steps, warmup=1, n=None, sort_interval=0, target_s=10.0):
         warmup = k + 1
     if steps is None:
         # the last warm-up step, past the first touch of the arrays
-        steps = int(min(200, max(2, round(target_s / max(per, 1e-6)))))
+        steps = int(min(200, max(10, round(target_s / max(per, 1e-6)))))
     t0 = time.perf_counter()
     for k in range(steps):
         o.step(sp, EB, J, buff, prm, warmup + k)
@@ -938,7 +938,7 @@ def main():
                     help="override the grid (smaller cases for profiling)")
     ap.add_argument("--e2e-steps", type=int, default=16)
     ap.add_argument("--cpu-steps", type=int, default=None,
-                    help="timed oracle steps of cpu_baseline (default: about 10 s of work)")
+                    help="timed oracle steps of cpu_baseline (default: about 10 s of work, at least 10 steps)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true",
