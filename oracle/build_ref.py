@@ -27,10 +27,11 @@ A second library per precision, oracle/_ref/libentity_ref_params_{f32,f64}.so,
 compiles oracle/ref_params.cpp with the reference's parameter sources
 (src/framework/parameters/*.cpp, src/global/utils/param_container.cpp,
 src/global/arch/kokkos_aliases.cpp) to run its own TOML-to-scales derivation.
-A third, oracle/_ref/libentity_ref_sort_{f32,f64}.so, compiles
-oracle/ref_sort.cpp with the reference's particle container and grid
+A third, oracle/_ref/libentity_ref_particles_{f32,f64}.so, compiles
+oracle/ref_particles.cpp with the reference's particle container and grid
 (src/framework/containers/particles.cpp, particles_sort.cpp,
-src/framework/domain/grid.cpp) to run its own RemoveDead and SortSpatially.
+src/framework/domain/grid.cpp) to run its own RemoveDead, SortSpatially and
+the output moments of ParticleMoments_kernel on that container.
 
 The reference checkout is located by $ENTITY_REFERENCE, else
 /root/reference. Without it, build() returns {} and the tests that need these
@@ -100,15 +101,16 @@ def build(verbose=False, jobs=None):
             todo.append(["g++", *_flags(root), "-O1", *defs, *psrc, "-o", target])
 
     # the reference's particle container and grid, for its own sort
-    # (Particles::RemoveDead and SortSpatially) driven by oracle/ref_sort.cpp
-    ssrc = [os.path.join(HERE, "ref_sort.cpp")]
+    # (Particles::RemoveDead and SortSpatially) and output moments, driven by
+    # oracle/ref_particles.cpp
+    ssrc = [os.path.join(HERE, "ref_particles.cpp")]
     ssrc += [os.path.join(root, "src", "framework", "containers", f)
              for f in ("particles.cpp", "particles_sort.cpp")]
     ssrc += [os.path.join(root, "src", "framework", "domain", "grid.cpp"),
              os.path.join(root, "src", "global", "arch", "kokkos_aliases.cpp")]
     for tag, defs in (("f32", ["-DSINGLE_PRECISION"]), ("f64", [])):
-        target = os.path.join(OUT, f"libentity_ref_sort_{tag}.so")
-        libs[("sort", tag)] = target
+        target = os.path.join(OUT, f"libentity_ref_particles_{tag}.so")
+        libs[("particles", tag)] = target
         if _stale(target, deps + ssrc[:1]):
             todo.append(["g++", *_flags(root), "-O1", *defs, *ssrc, "-o", target])
 

@@ -71,13 +71,16 @@ def lib(real, order):
     return _libs[key]
 
 
-def sort_lib(real):
-    key = ("sort", "f32" if real == torch.float32 else "f64")
+def particles_lib(real):
+    key = ("particles", "f32" if real == torch.float32 else "f64")
     if key not in _libs:
         paths = build_ref.build()
         if key not in paths:
             raise RuntimeError("the reference checkout is not available")
         L = C.CDLL(paths[key])
+        L.ref_output_moment.restype = C.c_int
+        L.ref_output_moment.argtypes = [C.POINTER(OrcGrid), C.POINTER(OrcSpecies)] + \
+            [C.c_int] * 6 + [C.c_double, C.c_double, C.c_void_p, C.c_int]
         L.ref_sort.restype = C.c_int64
         L.ref_sort.argtypes = [C.POINTER(OrcGrid), C.POINTER(OrcSpecies), C.c_int, C.c_void_p,
                                C.c_int, C.c_void_p, C.c_int]
@@ -137,12 +140,23 @@ class RefOracle(Oracle):
     def sync_currents(self, J, buff):
         _check(self.R.ref_sync_currents(C.byref(self.og), _p(J), _p(buff)))
 
+    def output_moment(self, species, mom, bckp, comp):
+        """ParticleMoments_kernel of the reference's container, as ComputeMoments
+        launches it; mom as Oracle.output_moment."""
+        S = particles_lib(self.g.real)
+        for sp in species:
+            s = self.species(sp)
+            _check(S.ref_output_moment(C.byref(self.og), C.byref(s), mom["id"], mom.get("c1", 0),
+                                       mom.get("c2", 0), mom.get("order", 0),
+                                       mom.get("smoothing", 2), int(mom.get("use_weights", 0)),
+                                       float(mom["inv_n0"]), float(mom["dx"]), _p(bckp), comp))
+
     def sort_particles(self, sp, remove_dead, pld_r=None, pld_i=None):
         """Particles::RemoveDead (when remove_dead) and SortSpatially of the
         reference's own particle container on the species, in place; the
         payloads (row-major particle x column tensors, pld_i int32) move with
         it. Returns the new particle count."""
-        S = sort_lib(self.g.real)
+        S = particles_lib(self.g.real)
         s = self.species(sp)
         nr = 0 if pld_r is None else pld_r.shape[1]
         ni = 0 if pld_i is None else pld_i.shape[1]

@@ -235,6 +235,36 @@ def test_conductor_walls_match_reference(dim, real, sides):
         assert torch.equal(Fa, Fb), (set_e, set_b)
 
 
+MOMENTS = [dict(id=0), dict(id=1), dict(id=2), dict(id=3), dict(id=4, c1=0, c2=0),
+           dict(id=4, c1=1, c2=2), dict(id=4, c1=3, c2=0), dict(id=5, c1=2)]
+
+
+@pytest.mark.parametrize("smooth", [(0, 2), (1, 2), (2, 2), (3, 2), (2, 1)])
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("dim", [2, 3])
+def test_output_moments_match_reference(dim, real, smooth):
+    # ParticleMoments_kernel<SRPIC, Minkowski, F, 6> over the reference's own
+    # container, as ComputeMoments launches it (serial scatter order), against
+    # the oracle's moments: Rho, Charge, N, Nppc, T^{00}, T^{12}, T^{30}, V2,
+    # with spline orders 0-3 and the constant window, each into a zeroed
+    # buffer as the writer zeroes it first (metadomain_io.cpp)
+    order, smoothing = smooth
+    g = _grid(dim, 2, real)
+    sp = make_species(g, 3, 0.4, 0.2, 17, charge=-1.0, mass=2.0)
+    sp.tag[::6] = 0
+    sp.w = (0.5 + torch.rand(sp.npart, generator=torch.Generator().manual_seed(2),
+                             dtype=torch.float64)).to(real)
+    o, r = Oracle(g), _ref(g)
+    for k, m in enumerate(MOMENTS):
+        mom = dict(m, order=order, smoothing=smoothing, use_weights=k % 2 == 0, inv_n0=0.25,
+                   dx=0.5)
+        ba = torch.zeros_like(random_fields(g, 60 + k))
+        bb = ba.clone()
+        o.output_moment([sp], mom, ba, k % 6)
+        r.output_moment([sp], mom, bb, k % 6)
+        assert torch.equal(ba, bb), mom
+
+
 @pytest.mark.parametrize("remove_dead", [False, True])
 @pytest.mark.parametrize("real", REALS)
 @pytest.mark.parametrize("dim", [2, 3])
