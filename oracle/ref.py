@@ -67,6 +67,7 @@ def lib(real, order):
         L.ref_communicate.argtypes = [G, V, C.c_int, C.c_int, C.c_int]
         L.ref_sync_currents.argtypes = [G, V, V]
         L.ref_conductor_walls.argtypes = [G, V, C.c_int, C.c_int]
+        L.ref_output_divergence.argtypes = [G, V, V, C.c_int, D]
         _libs[key] = L
     return _libs[key]
 
@@ -129,6 +130,9 @@ class RefOracle(Oracle):
     def gr_filter_pass(self, J, buff, axis_min=1, axis_max=1):
         _check(self.R.ref_filter_pass_axisym(C.byref(self.og), _p(J), _p(buff), axis_min,
                                              axis_max))
+
+    def output_divergence(self, EB, bckp, comp, dx=1.0):
+        _check(self.R.ref_output_divergence(C.byref(self.og), _p(EB), _p(bckp), comp, dx))
 
     def conductor_walls(self, EB, set_e, set_b):
         """The CONDUCTOR sides of the grid's field boundaries (set_field_bcs)."""

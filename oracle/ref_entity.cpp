@@ -27,6 +27,7 @@
 #include "kernels/fields_bcs.hpp"
 #include "kernels/currents_deposit.hpp"
 #include "kernels/digital_filter.hpp"
+#include "kernels/divergences.hpp"
 #include "kernels/faraday_mink.hpp"
 #include "kernels/pushers/gr.hpp"
 #include "kernels/pushers/sr.hpp"
@@ -420,6 +421,26 @@ namespace {
     }
   }
 
+  // ---- output: div E -------------------------------------------------------
+  // ComputeDivergence_kernel<Minkowski, 6> over the active cells into
+  // component `comp` of a 6-component buffer (metadomain_io.cpp:525-533)
+  template <Dimension D>
+  void divergence(const orc_grid* g, const void* EB, void* bckp, int comp, double dx) {
+    auto       em  = wrap_field<D, 6>(g, EB, g->em_s);
+    auto       out = wrap_field<D, 6>(g, bckp, g->em_s);
+    const auto metric = make_metric<D>(g, dx);
+    const std::int64_t ng = N_GHOSTS;
+    if constexpr (D == Dim::_2D) {
+      Kokkos::parallel_for(
+        Kokkos::MDRangePolicy<Kokkos::Rank<2>>({ ng, ng }, { ng + g->n1, ng + g->n2 }),
+        kernel::ComputeDivergence_kernel<metric::Minkowski<D>, 6>(metric, em, out, (idx_t)comp));
+    } else {
+      Kokkos::parallel_for(
+        Kokkos::MDRangePolicy<Kokkos::Rank<3>>({ ng, ng, ng }, { ng + g->n1, ng + g->n2, ng + g->n3 }),
+        kernel::ComputeDivergence_kernel<metric::Minkowski<D>, 6>(metric, em, out, (idx_t)comp));
+    }
+  }
+
   // ---- GR: metric::QKerrSchild<Dim::_2D> --------------------------------
   // mp = { x1min, x1max, x2min, x2max, a, r0, h }
   using QKS = metric::QKerrSchild<Dim::_2D>;
@@ -657,6 +678,13 @@ int ref_communicate(const orc_grid* g, void* fld, int is_em, int c0, int c1) {
       if (is_em) communicate<Dim::_3D, 6>(g, fld, g->em_s, c0, c1);
       else       communicate<Dim::_3D, 3>(g, fld, g->cur_s, c0, c1);
     });
+}
+
+// div E of EB into component comp of bckp (em layout), active cells
+int ref_output_divergence(const orc_grid* g, const void* EB, void* bckp, int comp, double dx) {
+  return dispatch(
+    g, [&] { divergence<Dim::_2D>(g, EB, bckp, comp, dx); },
+    [&] { divergence<Dim::_3D>(g, EB, bckp, comp, dx); });
 }
 
 // the perfect-conductor sides of g->fbc (2) on EB

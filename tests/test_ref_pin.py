@@ -235,6 +235,19 @@ def test_conductor_walls_match_reference(dim, real, sides):
         assert torch.equal(Fa, Fb), (set_e, set_b)
 
 
+@pytest.mark.parametrize("real", REALS)
+@pytest.mark.parametrize("dim", [2, 3])
+def test_output_divergence_matches_reference(dim, real):
+    # ComputeDivergence_kernel<Minkowski, 6> over the active cells
+    g = _grid(dim, 2, real)
+    EB = random_fields(g, 70)
+    ba, bb = random_fields(g, 71), None
+    bb = ba.clone()
+    Oracle(g).output_divergence(EB, ba, 2)
+    _ref(g).output_divergence(EB, bb, 2)
+    assert torch.equal(ba, bb)
+
+
 MOMENTS = [dict(id=0), dict(id=1), dict(id=2), dict(id=3), dict(id=4, c1=0, c2=0),
            dict(id=4, c1=1, c2=2), dict(id=4, c1=3, c2=0), dict(id=5, c1=2)]
 
