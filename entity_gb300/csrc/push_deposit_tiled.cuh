@@ -109,21 +109,36 @@ template <int D, typename real, int O>
 struct TileShape {
   // 2D: 16 x 8 cells. The 512^2 pair plasma (2 x 16 ppc) ran push+deposit in
   // 0.578 ms with 32 x 32 tiles (256 CTAs, 0.56 waves), 0.456 ms with
-  // 16 x 16, 0.419 ms with 16 x 8 and 0.429 ms with 8 x 8
-  static constexpr int X = 16, Y = 8, Z = 1, NT = 256;
+  // 16 x 16, 0.419 ms with 16 x 8 and 0.429 ms with 8 x 8.
+  // NT threads per CTA; MINB CTAs per SM asked of the register allocator.
+  // The kernel is latency-bound, so warps per SM pay: FP32 at 256 threads ran
+  // 0.543 ms with the allocator's 80 registers (3 CTAs/SM), 0.388 ms at 64
+  // (4 CTAs), 0.350 ms at 48 (5 CTAs, no spill) and 0.366 ms at 40 (6 CTAs,
+  // spilling); 512 threads x 2 gave 0.408 ms
+  static constexpr int X = 16, Y = 8, Z = 1, NT = 256,
+                       MINB = sizeof(real) == 4 ? (O == 3 ? 4 : 5) : 1;  // order 3 spills at 5
 };
 // 3D FP32 at order 3: 8^3 cells, so that two copies of the J window fit
 // (measured on the 96^3 sweep plasma, 2 x 32 ppc: 28.1 ms per step against
 // 34.7 ms with one copy and 16 x 8 x 4 tiles). At order 2 the copies did not
 // pay (50.5 against 48.1 ms on the 256^3 turbulence plasma, 2 x 8 ppc): its
 // warps span several cells, so fewer lanes share a word.
+// Threads per CTA: one CTA per SM (the shared memory), so the thread count
+// sets the warps that hide the kernel's latencies, and the register file
+// sets what each may use. Push+deposit of the 256^3 turbulence plasma
+// (order 2) took 44.96 ms at 512 threads (128 registers), 40.26 at 640 (96),
+// 38.38 at 768 (80), 38.19 at 896 (72) and 36.31 at 1024 (64, no spill); the
+// 96^3 sweep plasma (order 3) 27.00, 25.55, 25.62, 26.30 and 26.86 ms (at
+// 1024 its registers spill)
 template <int O>
 struct TileShape<3, float, O> {
-  static constexpr int X = (O == 3 ? 8 : 16), Y = 8, Z = 8, NT = 512;
+  static constexpr int X = (O == 3 ? 8 : 16), Y = 8, Z = 8, NT = (O == 3 ? 640 : 1024), MINB = 1;
 };
+// FP64 (8 x 8 x 4 cells): 256, 384, 512 and 768 threads ran the FP64 twin of
+// the sweep plasma (order 3) at 150, 151, 145 and 137 M particle-steps/s
 template <int O>
 struct TileShape<3, double, O> {
-  static constexpr int X = 8, Y = 8, Z = 4, NT = 256;
+  static constexpr int X = 8, Y = 8, Z = 4, NT = 384, MINB = 1;
 };
 
 // window halos (cells below / above the tile) of the interpolation and the
@@ -236,7 +251,7 @@ __device__ __forceinline__ int wrap_periodic(int x, int n) {
 }
 
 template <int D, int O, typename real>
-__global__ void __launch_bounds__(TileShape<D, real, O>::NT)
+__global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, O>::MINB)
     k_push_deposit_tiled(const __grid_constant__ TiledArgs<real> a) {
   using G               = TiledGeom<D, O, real>;
   using H               = Halo<O>;
