@@ -276,11 +276,11 @@ __global__ void __launch_bounds__(256) k_gr_island_list(GRPushArgs<real> a) {
 
 // The bulk: every live particle outside the island, in the field
 // precision. With a.list null (FP64 fields, or no island) every particle is
-// pushed here.
+// pushed here. It asks for three CTAs per SM (80 registers instead of the
+// allocator's 120, a 12-byte spill at order 2): the Wald problem's
+// push+deposit went from 0.718 to 0.608 ms per step; the island kernel at
+// four CTAs of 128 spilled and lost.
 template <int O, typename real>
-// three CTAs per SM (80 registers instead of the allocator's 120, a 12-byte
-// spill at order 2): the Wald problem's push+deposit went from 0.718 to
-// 0.608 ms per step; the island kernel at four CTAs of 128 spilled and lost
 __global__ void __launch_bounds__(256, 3) k_gr_push(GRPushArgs<real> a) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.sp.npart; p += stride) {
