@@ -64,6 +64,11 @@ struct pic_ctx {
   long long*                                      jfix       = nullptr;
   size_t                                          jfix_elems = 0;
   unsigned*                                       jfix_bound = nullptr;
+  // deposit records of the tiled kernel (3D FP32; allocated on first use):
+  // stage_slots buffers of pic::kStageCap records and their claim words
+  uint4*                                          stage_rec   = nullptr;
+  unsigned*                                       stage_claim = nullptr;
+  int                                             stage_slots = 0;
 };
 
 namespace pic_internal {

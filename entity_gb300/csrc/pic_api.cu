@@ -218,6 +218,31 @@ int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void
   a.write_prev = write_prev ? 1 : 0;
   a.err        = c->d_err;
   const int D = c->grid.dim, O = c->grid.order;
+  if (D == 3 && sizeof(real) == 4 && (O == 1 || O == 2)) {
+    // two buffers per SM: the launcher checks them against the kernel's
+    // occupancy and deposits directly when they do not suffice
+    if (!c->stage_rec) {
+      const int n = 2 * pic::sm_count();
+      if (cudaMalloc((void**)&c->stage_rec, sizeof(uint4) * 2 * (size_t)pic::kStageCap * n) !=
+              cudaSuccess ||
+          cudaMalloc((void**)&c->stage_claim, sizeof(unsigned) * (size_t)n) != cudaSuccess ||
+          cudaMemsetAsync(c->stage_claim, 0, sizeof(unsigned) * (size_t)n, s) != cudaSuccess) {
+        cudaGetLastError();
+        if (c->stage_rec) cudaFree(c->stage_rec);
+        if (c->stage_claim) cudaFree(c->stage_claim);
+        c->stage_rec   = nullptr;
+        c->stage_claim = nullptr;
+      } else {
+        c->stage_slots = n;
+      }
+    }
+    if (c->stage_rec) {
+      a.st.rec    = c->stage_rec;
+      a.st.claim  = c->stage_claim;
+      a.st.nslots = c->stage_slots;
+      a.st.cap    = pic::kStageCap;
+    }
+  }
   cudaError_t e = cudaErrorInvalidValue;
 #define PIC_TD(DD, OO) \
   if (D == DD && O == OO) e = pic::launch_push_deposit_tiled<DD, OO, real>(a, s);
@@ -396,6 +421,8 @@ int pic_destroy(pic_ctx* c) {
   cudaFree(c->gr_island_cnt);
   if (c->jfix) cudaFree(c->jfix);
   if (c->jfix_bound) cudaFree(c->jfix_bound);
+  if (c->stage_rec) cudaFree(c->stage_rec);
+  if (c->stage_claim) cudaFree(c->stage_claim);
   if (c->gr_fork) cudaEventDestroy(c->gr_fork);
   for (auto e : c->gr_join) cudaEventDestroy(e);
   for (auto q : c->gr_side) cudaStreamDestroy(q);

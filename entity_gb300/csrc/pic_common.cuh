@@ -157,6 +157,46 @@ __device__ __forceinline__ void for_deposit(int i_init, real di_init, int i_fin,
   }
 }
 
+// The first node of shape<O, false>'s support for the cell i and offset di:
+// i at order 1, i - 1 at order 3, and at order 2 the one the offset's half
+// of the cell selects (the same comparison shape makes)
+template <int O, typename real>
+__device__ __forceinline__ int shape_first_node(int i, real di) {
+  if constexpr (O == 2) return di < (real)0.5 ? i - 1 : i;
+  else                  return O == 3 ? i - 1 : i;
+}
+
+// true when for_deposit's initial and final supports start at the same node
+// along every simulated axis: the Esirkepov box is then O + 1 nodes wide on
+// each axis (for_deposit's third case), never O + 2
+template <int D, int O, typename real, typename P>
+__device__ __forceinline__ bool support_unmoved(const P& q) {
+  bool same = true;
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+    same = same && shape_first_node<O>(q.ip[a], (real)q.dxp[a]) ==
+                       shape_first_node<O>(q.i[a], (real)q.dx[a]);
+  return same;
+}
+
+// for_deposit when both supports start at the same node (support_unmoved):
+// its third case, with i_max = i_min + O known to the compiler's caller
+template <int O, typename real>
+__device__ __forceinline__ void for_deposit_unmoved(int i_init, real di_init, int i_fin,
+                                                    real di_fin, int& i_min, real* iS, real* fS) {
+  int  i_fin_min;
+  real iS_[O + 1], fS_[O + 1];
+  shape<O, false>(i_init, di_init, i_min, iS_);
+  shape<O, false>(i_fin, di_fin, i_fin_min, fS_);
+#pragma unroll
+  for (int j = 0; j < O + 1; j++) {
+    iS[j] = iS_[j];
+    fS[j] = fS_[j];
+  }
+  iS[O + 1] = (real)0;
+  fS[O + 1] = (real)0;
+}
+
 // ---------------------------------------------------------------------------
 // field access through a small view; ghost-inclusive indices
 // ---------------------------------------------------------------------------
@@ -443,7 +483,7 @@ __device__ __forceinline__ void move_and_bound(Prtl<real>& q, bool massive, real
 // outside the ghost-inclusive extents `ext` (possible only for moves longer
 // than the ghost layers allow, i.e. a time step beyond the CFL limit);
 // ext == nullptr skips the check (the caller guarantees the window).
-template <int D, int O, typename real, typename Add>
+template <int D, int O, typename real, bool UNMOVED = false, typename Add>
 __device__ __forceinline__ bool deposit_with_velocity(const Prtl<real>& q, const real* vp,
                                                       real weight, real charge, real inv_dt,
                                                       int ng, const int* ext, Add&& add);
@@ -473,11 +513,15 @@ __device__ __forceinline__ bool deposit_particle(const Prtl<real>& q, real weigh
 }
 
 // the deposit proper, given the particle velocity vp (the GR deposit passes
-// its metric velocity, currents_deposit.hpp:138-159)
-template <int D, int O, typename real, typename Add>
+// its metric velocity, currents_deposit.hpp:138-159). UNMOVED (orders 1-3):
+// the caller has checked support_unmoved, so every axis' box is O + 1 nodes
+// wide and the stencil's extent is known at compile time; the entries and
+// their values are those of the general form.
+template <int D, int O, typename real, bool UNMOVED, typename Add>
 __device__ __forceinline__ bool deposit_with_velocity(const Prtl<real>& q, const real* vp,
                                                       real weight, real charge, real inv_dt,
                                                       int ng, const int* ext, Add&& add) {
+  static_assert(!UNMOVED || O >= 1, "the zigzag deposit has no support box");
   const real ONE = 1, HALF = 0.5, INV_2 = 0.5;
   if constexpr (O == 0) {
     if (ext) {
@@ -554,12 +598,17 @@ __device__ __forceinline__ bool deposit_with_velocity(const Prtl<real>& q, const
     int           imin[3] = { 0, 0, 0 }, imax[3] = { 0, 0, 0 };
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      for_deposit<O>(q.ip[a], (real)q.dxp[a], q.i[a], (real)q.dx[a], imin[a], imax[a], iS[a], fS[a]);
+      if constexpr (UNMOVED) {
+        for_deposit_unmoved<O>(q.ip[a], (real)q.dxp[a], q.i[a], (real)q.dx[a], imin[a], iS[a], fS[a]);
+        imax[a] = imin[a] + O;
+      } else {
+        for_deposit<O>(q.ip[a], (real)q.dxp[a], q.i[a], (real)q.dx[a], imin[a], imax[a], iS[a], fS[a]);
+      }
       if (ext && (imin[a] + ng < 0 || imax[a] + ng >= ext[a])) return false;
     }
     const real THIRD = K<real>::THIRD;
     const real Q     = coeff * inv_dt;
-    const int  d1 = imax[0] - imin[0], d2 = imax[1] - imin[1];
+    const int  d1 = UNMOVED ? O : imax[0] - imin[0], d2 = UNMOVED ? O : imax[1] - imin[1];
     const int  i0 = imin[0] + ng, j0 = imin[1] + ng;
     // Every entry of the (O+2)-wide stencil is computed and only the add is
     // predicated on the stencil extent: the loops carry no divergent
@@ -608,7 +657,7 @@ __device__ __forceinline__ bool deposit_with_velocity(const Prtl<real>& q, const
         }
       }
     } else {
-      const int d3 = imax[2] - imin[2];
+      const int d3 = UNMOVED ? O : imax[2] - imin[2];
       const int k0 = imin[2] + ng;
       real      t0[N], t1[N], t2[N];  // THIRD * (fS - iS) per axis
 #pragma unroll

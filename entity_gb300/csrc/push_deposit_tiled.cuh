@@ -21,8 +21,8 @@
 // integers and 0.5 for double), and integer sums do not depend on the order
 // of the additions. Each tile scales contributions by a power of two 2^s so
 // that |v 2^s| < 2^b, rounds them to integers (exact up to the quantisation
-// 2^-s) and adds them as 32-bit words: X = 4096 hi + lo with lo = X mod 4096
-// (float), or three 16-bit words and a signed top word (double). With N
+// 2^-s) and adds them as 32-bit words: X modulo 2^32 and X >> 12 (float),
+// or three 16-bit words and a signed top word (double). With N
 // particles in the tile no cell takes more than N additions per component,
 // so b = min(30, 43 - log2 N) (float; 29 bits at 16k particles) or
 // b = 62 - log2 N (double) overflows neither a word nor the 64-bit total.
@@ -61,18 +61,22 @@ struct FixedAcc<float> {
   // b = 43 - log2 N keeps the high-word sums below 2^31; capped at 30 so that
   // the scaled contribution converts to a 32-bit integer
   __device__ static int bits(int64_t n) { return min(30, 43 - (n > 1 ? 64 - __clzll(n - 1) : 0)); }
-  // v arrives already scaled by 2^s (|v| < 2^b). X = round(v) is split as
-  // X = 4096 hi + lo with lo = X mod 4096 in [0, 4096) (unsigned) and hi the
-  // floored quotient; both words take integer adds, so each word's sum is
-  // exact and independent of the order of the additions.
+  // v arrives already scaled by 2^s (|v| < 2^b). X = round(v) goes into two
+  // words with integer adds: the low word sums X itself modulo 2^32, the
+  // high word sums the floored quotient hi = X >> 12. Over the N additions
+  // sum X = 4096 H + r with H the high word's total and r = sum (X mod 4096)
+  // in [0, 4096 N), below 2^32 for N <= NMAX; the low word fixes r modulo
+  // 2^32, so r = L - 4096 H (mod 2^32). Both sums are exact and independent
+  // of the order of the additions, and the low word needs no mask.
   __device__ static void add(unsigned* w, int plane, float v) {
     const int X = __float2int_rn(v);
-    atomicAdd(w, (unsigned)X & 4095u);
+    atomicAdd(w, (unsigned)X);
     atomicAdd(w + plane, (unsigned)(X >> 12));
   }
   __device__ static bool nonzero(const unsigned* w, int plane) { return (w[0] | w[plane]) != 0u; }
   __device__ static long long total(const unsigned* w, int plane) {
-    return (long long)(int)w[plane] * 4096 + (long long)w[0];
+    const unsigned H = w[plane];
+    return (long long)(int)H * 4096 + (long long)(w[0] - (H << 12));
   }
   __device__ static float to_real(long long t, float unscale) { return __ll2float_rn(t) * unscale; }
 };
@@ -161,6 +165,25 @@ struct TiledSpecies {
   unsigned*      ovf_count;
 };
 
+// Deposit records (3D FP32, orders 1 and 2). Most particles end a step with
+// both shape supports starting at the same node on every axis
+// (support_unmoved): their Esirkepov box is (O + 1) wide on each axis, a
+// stencil the compiler unrolls to its exact extent (54 of the 144 entries at
+// order 2). A warp deposits those at once. The others, whose box is O + 2
+// wide on some axis, are appended as 32-byte records to a buffer in global
+// memory (L2-resident: a few hundred KB per CTA, written and read back by
+// the same CTA) and deposited after the tile's pushes by full warps. So no
+// warp runs the wide stencil for one lane, and J is unchanged to the bit:
+// the window's integer sums do not depend on the order of the additions.
+// A CTA claims one of nslots buffers (nslots >= the CTAs that can be
+// resident at once); without one, or past cap records, it deposits at once.
+struct DepStage {
+  uint4*    rec    = nullptr;  // nslots * cap records of two uint4
+  unsigned* claim  = nullptr;  // nslots words: 0 free, 1 held
+  int       nslots = 0, cap = 0;
+};
+constexpr int kStageCap = 8192;  // records per buffer (256 KB)
+
 template <typename real>
 struct TiledArgs {
   TiledSpecies<real> s[kMaxTiledSpecies];
@@ -181,6 +204,8 @@ struct TiledArgs {
   // FP32: the exact 64-bit accumulator the tile sums are flushed into (null:
   // float atomics into J)
   FixedJ             fj;
+  // 3D FP32: where a tile's moved-support particles wait for their deposit
+  DepStage           st;
 };
 
 template <int D, int O, typename real>
@@ -201,6 +226,11 @@ struct TiledGeom {
   static constexpr int    WORDS      = FixedAcc<real>::WORDS;
   static constexpr int    PLANE      = 3 * NJ;
   static constexpr int    COPIES     = (D == 3 && sizeof(real) == 4 && O == 3) ? 2 : 1;
+  // moved-support particles deposited from records (DepStage). Not at order
+  // 3: its box shrinks only from 5^3 to 4^3, and the sweep plasma (theta = 1,
+  // 8^3-cell tiles of 2 x 32 ppc) moves 40 % of its supports, more than a
+  // buffer holds; push+deposit on 96^3 went from 25.0 to 27.5 ms
+  static constexpr bool   STAGE      = D == 3 && sizeof(real) == 4 && (O == 1 || O == 2);
   // the copies start 16 banks apart: one word in both copies falls in
   // two different banks
   static constexpr int    COPY       = WORDS * PLANE + ((16 - (WORDS * PLANE) % 32) + 32) % 32;
@@ -264,6 +294,8 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
   real*          Jr  = reinterpret_cast<real*>(Jw);  // real_t accumulation of dense tiles
   __shared__ unsigned int s_qmax;  // bit pattern of the tile's largest |q w| max(1/dt, 1)
   __shared__ __align__(8) unsigned long long s_bar;  // completion of the E-window load
+  __shared__ int      s_slot;  // the claimed record buffer, -1 for none
+  __shared__ unsigned s_nrec;  // records appended so far
 
   const int t  = blockIdx.x + a.tile0;
   const int tx = t % a.ntiles[0];
@@ -327,7 +359,22 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
     Jw[idx] = 0u;
   // largest contribution bound of the tile, |q w| max(1/dt, 1), and its
   // particle count (an upper bound on the additions any cell receives)
-  if (threadIdx.x == 0) s_qmax = 0u;
+  if (threadIdx.x == 0) {
+    s_qmax = 0u;
+    s_nrec = 0u;
+    s_slot = -1;
+    if (G::STAGE && a.st.rec) {
+      // one attempt per buffer, starting where this CTA's predecessors by
+      // index left theirs: no wait
+      for (int k = 0; k < a.st.nslots; ++k) {
+        const int sl = (int)((blockIdx.x + (unsigned)k) % (unsigned)a.st.nslots);
+        if (atomicCAS(a.st.claim + sl, 0u, 1u) == 0u) {
+          s_slot = sl;
+          break;
+        }
+      }
+    }
+  }
   __syncthreads();
   // (with the exact global accumulator the bound is the call's, known already)
   const bool global_unit = sizeof(real) == 4 && a.fj.p != nullptr;
@@ -363,13 +410,24 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
     // any thread) abandons the tile on all of them and is counted
     const bool done = mbar_wait_bounded(bar, 0u);
     if (__syncthreads_or(!done)) {
-      if (threadIdx.x == 0) atomicAdd(a.err + ERR_WAIT_TIMEOUT, 1ull);
+      if (threadIdx.x == 0) {
+        atomicAdd(a.err + ERR_WAIT_TIMEOUT, 1ull);
+        if (s_slot >= 0) atomicExch(a.st.claim + s_slot, 0u);
+      }
       return;
     }
   }
   const SmemView<real> ebv{ EBs, g0[0] - R, g0[1], g0[2], G::WEX, G::WEX * G::WEY, G::NE };
   const int joff[3] = { ng + T0[0] - H::J_LO, ng + T0[1] - H::J_LO,
                         D == 3 ? ng + T0[2] - H::J_LO : 0 };
+  const int jb      = -joff[0] - joff[1] * G::WJ0 - joff[2] * (G::WJ0 * G::WJ1);
+  const int slot    = s_slot;
+  uint4*    recs    = slot >= 0 ? a.st.rec + (size_t)slot * a.st.cap * 2 : nullptr;
+  const real vz[3]  = { 0, 0, 0 };  // the 3D Esirkepov deposit reads no velocity
+  // cell of a record relative to the tile: 8 bits per axis, offset by 64
+  static_assert(G::TX + kDriftMargin + 2 < 64 && G::TY + kDriftMargin + 2 < 64 &&
+                    G::TZ + kDriftMargin + 2 < 64,
+                "record cells are 8-bit offsets from the tile origin");
 
   // 2. particles of the tile, species by species
   for (int s = 0; s < a.nsp; ++s) {
@@ -465,23 +523,87 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
       }
       // in fixed point the weight carries the power-of-two scale, so every
       // contribution arrives scaled exactly (w 2^s rounds like w)
-      const int  jb = -joff[0] - joff[1] * G::WJ0 - joff[2] * (G::WJ0 * G::WJ1);
       const real wp = fixed ? w[p] * scale : w[p];
       // Shared-memory atomics serialise the lanes of a warp that hit one
       // word, and cell-sorted lanes share their boxes: odd and even lanes
       // add to separate copies, which halves those collisions. The flush
       // sums the copies' integer totals, so J is unchanged to the bit.
-      unsigned* Jc = Jw + (G::COPIES == 2 ? (int)(threadIdx.x & 1) * G::COPY : 0);
-      deposit_particle<D, O, real>(q, wp, S.charge, a.inv_dt, a.dx, ng, nullptr,
-                                   [&](int i, int j, int k, int c, real v) {
-                                     const int e = jb + i + j * G::WJ0 +
-                                                   k * (G::WJ0 * G::WJ1) + c * G::NJ;
-                                     if (fixed) FA::add(Jc + e, G::PLANE, v);
-                                     else       atomicAdd(Jr + e, v);
-                                   });
+      unsigned* Jc  = Jw + (G::COPIES == 2 ? (int)(threadIdx.x & 1) * G::COPY : 0);
+      auto      add = [&](int i, int j, int k, int c, real v) {
+        const int e = jb + i + j * G::WJ0 + k * (G::WJ0 * G::WJ1) + c * G::NJ;
+        if (fixed) FA::add(Jc + e, G::PLANE, v);
+        else       atomicAdd(Jr + e, v);
+      };
+      if constexpr (G::STAGE) {
+        if (recs) {
+          if (support_unmoved<D, O, real>(q)) {
+            deposit_with_velocity<D, O, real, true>(q, vz, wp, S.charge, a.inv_dt, ng, nullptr,
+                                                    add);
+            continue;
+          }
+          // a record needs the move to stay within one cell per axis
+          bool one = true;
+#pragma unroll
+          for (int d = 0; d < D; ++d) one = one && q.ip[d] - q.i[d] >= -1 && q.ip[d] - q.i[d] <= 1;
+          const unsigned ball = __ballot_sync(__activemask(), one);
+          if (one) {
+            const int lane   = threadIdx.x & 31;
+            const int leader = __ffs(ball) - 1;
+            unsigned  base   = 0;
+            if (lane == leader) base = atomicAdd(&s_nrec, (unsigned)__popc(ball));
+            base             = __shfl_sync(ball, base, leader);
+            const unsigned r = base + __popc(ball & ((1u << lane) - 1u));
+            if (r < (unsigned)a.st.cap) {
+              unsigned cells = 0;
+#pragma unroll
+              for (int d = 0; d < D; ++d)
+                cells |= ((unsigned)(q.i[d] - T0[d] + 64) << (8 * d)) |
+                         ((unsigned)(q.ip[d] - q.i[d] + 1) << (24 + 2 * d));
+              const float coeff = (float)(wp * S.charge);
+              __stcg(recs + 2 * r, make_uint4(cells, __float_as_uint(q.dx[0]),
+                                              __float_as_uint(q.dx[1]), __float_as_uint(q.dx[2])));
+              __stcg(recs + 2 * r + 1,
+                     make_uint4(__float_as_uint(q.dxp[0]), __float_as_uint(q.dxp[1]),
+                                __float_as_uint(q.dxp[2]), __float_as_uint(coeff)));
+              continue;
+            }
+          }
+        }
+      }
+      deposit_particle<D, O, real>(q, wp, S.charge, a.inv_dt, a.dx, ng, nullptr, add);
     }
   }
   __syncthreads();
+  if constexpr (G::STAGE) {
+    // the recorded particles, 32 per warp; the record's coefficient is the
+    // product weight * charge that the direct deposit forms, times charge 1
+    if (recs) {
+      const int nrec = min((int)s_nrec, a.st.cap);
+      unsigned* Jc   = Jw + (G::COPIES == 2 ? (int)(threadIdx.x & 1) * G::COPY : 0);
+      auto      add  = [&](int i, int j, int k, int c, real v) {
+        const int e = jb + i + j * G::WJ0 + k * (G::WJ0 * G::WJ1) + c * G::NJ;
+        if (fixed) FA::add(Jc + e, G::PLANE, v);
+        else       atomicAdd(Jr + e, v);
+      };
+      for (int r = threadIdx.x; r < nrec; r += NT) {
+        const uint4 u0 = __ldcg(recs + 2 * r), u1 = __ldcg(recs + 2 * r + 1);
+        Prtl<real>  q;
+        const float dx[3]  = { __uint_as_float(u0.y), __uint_as_float(u0.z), __uint_as_float(u0.w) };
+        const float dxp[3] = { __uint_as_float(u1.x), __uint_as_float(u1.y), __uint_as_float(u1.z) };
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          q.i[d]   = (int)((u0.x >> (8 * d)) & 255u) - 64 + T0[d];
+          q.ip[d]  = q.i[d] + (int)((u0.x >> (24 + 2 * d)) & 3u) - 1;
+          q.dx[d]  = dx[d];
+          q.dxp[d] = dxp[d];
+        }
+        deposit_with_velocity<D, O, real>(q, vz, (real)__uint_as_float(u1.w), (real)1, a.inv_dt,
+                                          ng, nullptr, add);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && slot >= 0) atomicExch(a.st.claim + slot, 0u);
+  }
 
   // 3. flush the J window (periodic images folded onto active cells)
   for (int idx = threadIdx.x; idx < 3 * G::NJ; idx += NT) {

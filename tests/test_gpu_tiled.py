@@ -236,3 +236,42 @@ def test_exact_current_accumulation_adds_to_J():
                      flags=abi.PIC_PD_WRITE_PREV)
     torch.cuda.synchronize()
     assert torch.equal(Ja, J0 + Jz)
+
+
+@pytest.mark.parametrize("order,ppc,temp", [(1, 4, 0.3), (2, 4, 0.05), (2, 4, 2.0),
+                                            (1, 12, 2.0), (2, 12, 2.0)])
+def test_deposit_records_leave_J_unchanged(order, ppc, temp, monkeypatch):
+    """3D FP32, orders 1 and 2: the particles whose shape support moved are
+    deposited from records after the tile's pushes, the others at once
+    through the narrow stencil. J is the same to the bit as with every particle deposited at
+    once (ENTITY_PIC_NO_RECORDS=1), because the window's integer sums do not
+    depend on the order of the additions; the particles are identical. The
+    hot 2 x 12 ppc cases fill a tile's record buffer past its capacity, so
+    the particles beyond it are deposited at once as well."""
+    g = GridSpec(dim=3, n=(32, 16, 16), order=order, real=torch.float32)
+    EB = random_fields(g, 37, amp=0.1).cuda()
+    ctx = Context(g)
+    gpu = []
+    for k, sd in enumerate((81, 82)):
+        s = make_species(g, ppc, temp, 0.3 if k == 0 else -0.3, sd,
+                         charge=-1.0 if k == 0 else 1.0, index=k + 1).to("cuda")
+        assert ctx.sort(s, abi.PIC_SORT_SPATIAL | abi.PIC_SORT_TILED) == abi.PIC_OK
+        gpu.append(s)
+    runs = []
+    for off in ("0", "1"):
+        monkeypatch.setenv("ENTITY_PIC_NO_RECORDS", off)
+        sp = [s.clone() for s in gpu]
+        Js = []
+        for _ in range(2):
+            Jg = empty_field(g, 3, "cuda")
+            ctx.push_deposit(sp, EB, Jg, 0.45, 0.7, g.dx, flags=abi.PIC_PD_WRITE_PREV)
+            Js.append(Jg)
+        torch.cuda.synchronize()
+        runs.append((sp, Js))
+    for Ja, Jb in zip(runs[0][1], runs[1][1]):
+        assert torch.equal(Ja, Jb)
+        assert float(Ja.abs().max()) > 0
+    for a, b in zip(runs[0][0], runs[1][0]):
+        _assert_particles_equal(a.to("cpu"), b, 3)
+    assert ctx.device_errors() == [0, 0, 0, 0]
+    assert ctx.wait_timeouts() == 0
