@@ -144,6 +144,14 @@ template cudaError_t exclusive_scan<int32_t, int32_t>(const int32_t*, int64_t, i
 
 namespace {
 
+// Place of the cell lx within its tile row: the even cells first, then the
+// odd ones. A warp's lanes then cover cells two apart, whose order-2 support
+// boxes never start on the same node, so fewer of their J-window atomics
+// fall on one word; the window reads stay in distinct banks.
+__device__ __forceinline__ int tile_row_slot(int lx, int tx) {
+  return (lx & 1) ? (tx + 1) / 2 + lx / 2 : lx / 2;
+}
+
 // 1. keys + counts + provisional rank
 __global__ void k_keys(SortArgs a) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -165,7 +173,8 @@ __global__ void k_keys(SortArgs a) {
         const int tx = i1 / a.tile[0], ty = i2 / a.tile[1], tz = i3 / a.tile[2];
         const int lx = i1 - tx * a.tile[0], ly = i2 - ty * a.tile[1], lz = i3 - tz * a.tile[2];
         const int t  = (tz * a.ntiles[1] + ty) * a.ntiles[0] + tx;
-        key = (t * a.tile[2] + lz) * (a.tile[0] * a.tile[1]) + ly * a.tile[0] + lx;
+        key = (t * a.tile[2] + lz) * (a.tile[0] * a.tile[1]) + ly * a.tile[0] +
+              tile_row_slot(lx, a.tile[0]);
       } else if (a.dim == 2) {
         key = i1 * a.n[1] + i2;
       } else {

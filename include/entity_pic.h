@@ -65,7 +65,8 @@ extern "C" {
 #define PIC_SORT_SKIP_PREV 2u   /* leave i*_prev / dx*_prev arrays unpermuted */
 #define PIC_SORT_SPATIAL 4u     /* Particles::SortSpatially */
 /* With PIC_SORT_SPATIAL: order by tile of cells first, then by cell inside
- * the tile (cells inside a tile i1-fastest), instead of the reference's
+ * the tile (cells inside a tile i1-fastest, each row's even cells before its
+ * odd ones), instead of the reference's
  * i1-major cell key. The context then remembers each species' tile offsets
  * and pic_push_deposit runs the tiled kernel for it until the species' npart
  * changes or it is sorted again with another key. No reference counterpart:

@@ -1205,7 +1205,8 @@ static void permute_all(const orc_grid* g, orc_species* sp, const int64_t* perm)
 
 /* tile: NULL for the reference's cell key, else the tile shape of the
  * tile-major key (tile index i1-fastest over tiles, then the cell inside the
- * tile i1-fastest) that the GPU's tiled sort uses */
+ * tile i1-fastest, a row's even cells before its odd ones) that the GPU's
+ * tiled sort uses */
 static void sort_keyed(const orc_grid* g, orc_species* sp, const int* tile, int64_t* perm) {
   const int64_t np    = sp->npart;
   int           nt[3] = { 1, 1, 1 }, ts[3] = { 1, 1, 1 };
@@ -1226,7 +1227,9 @@ static void sort_keyed(const orc_grid* g, orc_species* sp, const int* tile, int6
     } else if (tile) {
       const int     c[3] = { sp->i1[p], sp->i2[p], g->dim == 3 ? sp->i3[p] : 0 };
       const int64_t t    = ((int64_t)(c[2] / ts[2]) * nt[1] + c[1] / ts[1]) * nt[0] + c[0] / ts[0];
-      key[p] = ((t * ts[2] + c[2] % ts[2]) * ts[1] + c[1] % ts[1]) * ts[0] + c[0] % ts[0];
+      /* within a tile row the even cells come first, then the odd ones */
+      const int lx = c[0] % ts[0], slot = (lx & 1) ? (ts[0] + 1) / 2 + lx / 2 : lx / 2;
+      key[p] = ((t * ts[2] + c[2] % ts[2]) * ts[1] + c[1] % ts[1]) * ts[0] + slot;
     } else if (g->dim == 2) {
       key[p] = (int64_t)sp->i1[p] * g->n2 + sp->i2[p];
     } else {
