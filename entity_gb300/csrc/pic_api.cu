@@ -1,6 +1,7 @@
 // C ABI of the particle-in-cell hot path: argument validation, dispatch to
 // the templated kernels by (dimension, shape order, precision), the device
 // error word, and the context's persistent scratch.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
@@ -218,6 +219,15 @@ int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void
   a.write_prev = write_prev ? 1 : 0;
   a.err        = c->d_err;
   const int D = c->grid.dim, O = c->grid.order;
+  {
+    // lanes of a warp over about four cells: the stride from the species'
+    // mean particles per cell
+    int64_t np = 0, cells = 1;
+    for (int k = 0; k < a.nsp; ++k) np += sps[k]->npart;
+    for (int d = 0; d < D; ++d) cells *= c->grid.n[d];
+    const int64_t ppc = np / std::max<int64_t>(1, (int64_t)a.nsp * cells);
+    a.lane_stride     = ppc >= 24 ? 4 : (ppc >= 12 ? 2 : 1);
+  }
   if (D == 3 && sizeof(real) == 4 && (O == 1 || O == 2)) {
     // two buffers per SM: the launcher checks them against the kernel's
     // occupancy and deposits directly when they do not suffice

@@ -206,6 +206,14 @@ struct TiledArgs {
   FixedJ             fj;
   // 3D FP32: where a tile's moved-support particles wait for their deposit
   DepStage           st;
+  // warps taken lane_stride at a time read their particles interleaved
+  // (1, 2 or 4; a divisor of the CTA's warps). A warp of a cell-sorted tile
+  // then spans 32 lane_stride / ppc cells; about four measured best: on
+  // the 256^3 turbulence plasma (8 ppc per species) strides 1, 2 and 4 took
+  // 28.9, 29.6 and 30.4 ms of push+deposit, on the 96^3 sweep plasma (32)
+  // 24.1, 21.2 and 20.4 ms, on the 512^2 pair plasma (16) 0.333, 0.323 and
+  // 0.330 ms
+  int                lane_stride = 1;
 };
 
 template <int D, int O, typename real>
@@ -422,6 +430,14 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
                         D == 3 ? ng + T0[2] - H::J_LO : 0 };
   const int jb      = -joff[0] - joff[1] * G::WJ0 - joff[2] * (G::WJ0 * G::WJ1);
   const int slot    = s_slot;
+  // The thread's particle within each NT-particle chunk. With lane_stride
+  // ls, ls consecutive warps share 32 ls consecutive particles, lane l of the
+  // group's k-th warp taking particle ls l + k: each warp spans ls times as
+  // many cells, so fewer of its lanes add to one J word, and the group
+  // still reads whole lines.
+  const int ls      = a.lane_stride;
+  const int wid     = (int)(threadIdx.x >> 5);
+  const int local   = (wid / ls) * (32 * ls) + ls * (int)(threadIdx.x & 31) + wid % ls;
   uint4*    recs    = slot >= 0 ? a.st.rec + (size_t)slot * a.st.cap * 2 : nullptr;
   const real vz[3]  = { 0, 0, 0 };  // the 3D Esirkepov deposit reads no velocity
   // cell of a record relative to the tile: 8 bits per axis, offset by 64
@@ -439,7 +455,7 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
     float*         da[3]  = { S.sp.dx1, S.sp.dx2, S.sp.dx3 };
     float*         dpa[3] = { S.sp.dx1p, S.sp.dx2p, S.sp.dx3p };
     const int64_t  lo = S.tile_start[t], hi = S.tile_start[t + 1];
-    for (int64_t p = lo + threadIdx.x; p < hi; p += NT) {
+    for (int64_t p = lo + local; p < hi; p += NT) {
       Prtl<real> q;
       q.tag = S.sp.tag[p];
       if (q.tag != PIC_TAG_ALIVE) {

@@ -275,3 +275,27 @@ def test_deposit_records_leave_J_unchanged(order, ppc, temp, monkeypatch):
         _assert_particles_equal(a.to("cpu"), b, 3)
     assert ctx.device_errors() == [0, 0, 0, 0]
     assert ctx.wait_timeouts() == 0
+
+
+@pytest.mark.parametrize("dim,order", [(3, 2), (3, 3), (2, 1)])
+def test_lane_stride_leaves_results_unchanged(dim, order, monkeypatch):
+    """Which thread pushes which particle of a tile (ENTITY_PIC_LANE_STRIDE:
+    1, 2 or 4 warps reading their particles interleaved) changes neither the
+    particles nor the exactly accumulated FP32 J."""
+    n = (40, 24, 16) if dim == 3 else (96, 64, 1)
+    g = GridSpec(dim=dim, n=n, order=order, real=torch.float32)
+    EB = random_fields(g, 43, amp=0.1).cuda()
+    ctx, gpu, _ = _tiled_pair(g, [91, 92], temp=0.3)
+    runs = []
+    for ls in ("1", "2", "4"):
+        monkeypatch.setenv("ENTITY_PIC_LANE_STRIDE", ls)
+        sp = [s.clone() for s in gpu]
+        Jg = empty_field(g, 3, "cuda")
+        ctx.push_deposit(sp, EB, Jg, 0.45, 0.7, g.dx, flags=abi.PIC_PD_WRITE_PREV)
+        torch.cuda.synchronize()
+        runs.append((sp, Jg))
+    for sp, Jg in runs[1:]:
+        assert torch.equal(Jg, runs[0][1])
+        for a, b in zip(runs[0][0], sp):
+            _assert_particles_equal(a.to("cpu"), b, dim)
+    assert ctx.device_errors() == [0, 0, 0, 0]
