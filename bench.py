@@ -95,21 +95,22 @@ BYTES_PER_CELL = 24 + 12
 
 # DRAM bytes (read + write) per particle of one k_push_deposit_tiled launch,
 # from an ncu capture of the same plasma on a 96^3 box (14,155,776 particles:
-# 637.1 MB read + 467.1 MB written); traffic grows with the particle count at
+# 652.1 MB read + 510.3 MB written, the deposit records' lines that leave L2
+# before they are read included); traffic grows with the particle count at
 # fixed particles per cell, so it scales to the full box by npart
-DRAM_BYTES_PER_PARTICLE = {"turb3d": 1125.71e6 / 14155776}
+DRAM_BYTES_PER_PARTICLE = {"turb3d": 1162.41e6 / 14155776}
 
 # what binds the dominant kernel beside HBM, from one `ncu --set full` capture
 # of the same kernel on a smaller box of the same plasma: instruction issue
 # and the shared-memory (l1tex) pipe that carries the fixed-point J atomics
 PIPE_LIMITS = {
-    "turb3d": {"issue_active_pct": 73.3, "l1tex_shared_atomic_wavefronts_per_particle": 22.0,
-               "l1tex_wavefronts_pct": 67.9, "warps_active_pct": 49.9,
-               "thread_instructions_per_particle": 3292,
-               "fp32_flops_per_particle": 1481,
+    "turb3d": {"issue_active_pct": 68.7, "l1tex_shared_atomic_wavefronts_per_particle": 16.6,
+               "l1tex_wavefronts_pct": 75.9, "warps_active_pct": 49.7,
+               "thread_instructions_per_particle": 2426,
+               "fp32_flops_per_particle": 1129,
                "capture": "ncu --set full, one launch on a 96^3 box of the same plasma"},
-    "sweep3d": {"issue_active_pct": 47.2, "l1tex_throughput_pct": 72.2,
-                "l1tex_shared_atomic_wavefronts_per_particle": 81.9,
+    "sweep3d": {"issue_active_pct": 55.7, "l1tex_wavefronts_pct": 52.7,
+                "l1tex_shared_atomic_wavefronts_per_particle": 50.1, "warps_active_pct": 31.4,
                 "capture": "ncu --set full, one launch on a 48^3 box of the same plasma"},
 }
 

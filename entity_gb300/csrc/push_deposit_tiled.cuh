@@ -184,6 +184,12 @@ struct DepStage {
 };
 constexpr int kStageCap = 8192;  // records per buffer (256 KB)
 
+// drops the 128-byte line at p (128-byte aligned) from L2 without writing it
+// back; its contents are undefined until written again
+__device__ __forceinline__ void discard_l2_line(const void* p) {
+  asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
+}
+
 template <typename real>
 struct TiledArgs {
   TiledSpecies<real> s[kMaxTiledSpecies];
@@ -615,6 +621,14 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
         }
         deposit_with_velocity<D, O, real>(q, vz, (real)__uint_as_float(u1.w), (real)1, a.inv_dt,
                                           ng, nullptr, add);
+        // Lanes 4m..4m+3 have read the four records of one 128-byte line and
+        // used them: the line is dropped from L2 unwritten, so the records
+        // cost no DRAM traffic (the next CTA on this buffer writes before it
+        // reads)
+        const int      base = r - (int)(threadIdx.x & 31);
+        const unsigned m    = nrec - base >= 32 ? 0xffffffffu : (1u << (nrec - base)) - 1u;
+        __syncwarp(m);
+        if ((r & 3) == 0) discard_l2_line(recs + 2 * r);
       }
     }
     __syncthreads();
