@@ -228,12 +228,13 @@ int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void
     const int64_t ppc = np / std::max<int64_t>(1, (int64_t)a.nsp * cells);
     a.lane_stride     = ppc >= 24 ? 4 : (ppc >= 12 ? 2 : 1);
   }
-  if (D == 3 && sizeof(real) == 4 && (O == 1 || O == 2)) {
+  if (D == 3 && sizeof(real) == 4 && O >= 1) {
     // two buffers per SM: the launcher checks them against the kernel's
     // occupancy and deposits directly when they do not suffice
+    const int cap = O == 3 ? 2 * pic::kStageCap : pic::kStageCap;
     if (!c->stage_rec) {
       const int n = 2 * pic::sm_count();
-      if (cudaMalloc((void**)&c->stage_rec, sizeof(uint4) * 2 * (size_t)pic::kStageCap * n) !=
+      if (cudaMalloc((void**)&c->stage_rec, sizeof(uint4) * 2 * (size_t)cap * n) !=
               cudaSuccess ||
           cudaMalloc((void**)&c->stage_claim, sizeof(unsigned) * (size_t)n) != cudaSuccess ||
           cudaMemsetAsync(c->stage_claim, 0, sizeof(unsigned) * (size_t)n, s) != cudaSuccess) {
@@ -250,7 +251,7 @@ int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void
       a.st.rec    = c->stage_rec;
       a.st.claim  = c->stage_claim;
       a.st.nslots = c->stage_slots;
-      a.st.cap    = pic::kStageCap;
+      a.st.cap    = cap;
     }
   }
   cudaError_t e = cudaErrorInvalidValue;

@@ -165,7 +165,7 @@ struct TiledSpecies {
   unsigned*      ovf_count;
 };
 
-// Deposit records (3D FP32, orders 1 and 2). Most particles end a step with
+// Deposit records (3D FP32, orders 1-3). Most particles end a step with
 // both shape supports starting at the same node on every axis
 // (support_unmoved): their Esirkepov box is (O + 1) wide on each axis, a
 // stencil the compiler unrolls to its exact extent (54 of the 144 entries at
@@ -182,7 +182,7 @@ struct DepStage {
   unsigned* claim  = nullptr;  // nslots words: 0 free, 1 held
   int       nslots = 0, cap = 0;
 };
-constexpr int kStageCap = 8192;  // records per buffer (256 KB)
+constexpr int kStageCap = 8192;  // records per buffer (256 KB), twice that at order 3
 
 // drops the 128-byte line at p (128-byte aligned) from L2 without writing it
 // back; its contents are undefined until written again
@@ -242,11 +242,12 @@ struct TiledGeom {
   static constexpr int    WORDS      = FixedAcc<real>::WORDS;
   static constexpr int    PLANE      = 3 * NJ;
   static constexpr int    COPIES     = (D == 3 && sizeof(real) == 4 && O == 3) ? 2 : 1;
-  // moved-support particles deposited from records (DepStage). Not at order
-  // 3: its box shrinks only from 5^3 to 4^3, and the sweep plasma (theta = 1,
-  // 8^3-cell tiles of 2 x 32 ppc) moves 40 % of its supports, more than a
-  // buffer holds; push+deposit on 96^3 went from 25.0 to 27.5 ms
-  static constexpr bool   STAGE      = D == 3 && sizeof(real) == 4 && (O == 1 || O == 2);
+  // moved-support particles deposited from records (DepStage), orders 1-3.
+  // At order 3 the buffers hold twice the records: the sweep plasma
+  // (theta = 1, 8^3-cell tiles of 2 x 32 ppc) moves 40 % of its supports;
+  // with 8192 records per buffer its push+deposit on 96^3 went from 25.0 to
+  // 27.5 ms, with 16384 (and the lane stride) from 20.5 to 19.6 ms
+  static constexpr bool   STAGE      = D == 3 && sizeof(real) == 4 && O >= 1;
   // the copies start 16 banks apart: one word in both copies falls in
   // two different banks
   static constexpr int    COPY       = WORDS * PLANE + ((16 - (WORDS * PLANE) % 32) + 32) % 32;

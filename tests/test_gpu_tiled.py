@@ -239,15 +239,17 @@ def test_exact_current_accumulation_adds_to_J():
 
 
 @pytest.mark.parametrize("order,ppc,temp", [(1, 4, 0.3), (2, 4, 0.05), (2, 4, 2.0),
-                                            (1, 12, 2.0), (2, 12, 2.0)])
+                                            (3, 4, 0.3), (1, 12, 2.0), (2, 12, 2.0),
+                                            (3, 24, 2.0)])
 def test_deposit_records_leave_J_unchanged(order, ppc, temp, monkeypatch):
-    """3D FP32, orders 1 and 2: the particles whose shape support moved are
+    """3D FP32, orders 1-3: the particles whose shape support moved are
     deposited from records after the tile's pushes, the others at once
     through the narrow stencil. J is the same to the bit as with every particle deposited at
     once (ENTITY_PIC_NO_RECORDS=1), because the window's integer sums do not
     depend on the order of the additions; the particles are identical. The
-    hot 2 x 12 ppc cases fill a tile's record buffer past its capacity, so
-    the particles beyond it are deposited at once as well."""
+    hot 2 x 12 ppc (orders 1-2) and 2 x 24 ppc (order 3) cases fill a tile's
+    record buffer past its capacity, so the particles beyond it are
+    deposited at once as well."""
     g = GridSpec(dim=3, n=(32, 16, 16), order=order, real=torch.float32)
     EB = random_fields(g, 37, amp=0.1).cuda()
     ctx = Context(g)
