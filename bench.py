@@ -442,8 +442,9 @@ def run_ours(args, w):
 
     # end to end through pic_srpic_step_host with host buffers: every step
     # copies the state in from pinned host memory (EB and each species' i, dx,
-    # u, w, tag) and the result out (the same plus J); the pipe overlaps one
-    # step's outgoing copies with the next step's incoming ones
+    # u, w, tag) and the result out (the same plus J, w only on steps that
+    # sort); the pipe overlaps one step's outgoing copies with the next step's
+    # incoming ones. The byte counts are means over the timed steps.
     e2e = None
     if not args.no_e2e:
         from entity_gb300.inputs import SpeciesArrays
@@ -461,13 +462,16 @@ def run_ours(args, w):
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
         a0.record()
+        nin = nout = 0
         for k in range(k2):
             ctx.step_host(pipe, hsp, sp, hEB, EB, hJ, J, buff, prm, args.warmup + args.steps + k)
+            bi, bo = pipe.bytes()  # counted as queued: steps that sort copy the weights out too
+            nin, nout = nin + bi, nout + bo
         pipe.sync()
         a1.record()
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-        nin, nout = pipe.bytes()
+        nin, nout = nin // k2, nout // k2
         pipe.close()
         barrier()
         te, _ = reduce_over_ranks(max(a0.elapsed_time(a1) / 1e3, 1e-9), 0, world, "cuda")

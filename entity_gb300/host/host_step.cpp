@@ -3,7 +3,8 @@
 //
 // Every call copies the step's inputs in (EB and each species' i, dx, u,
 // weight, tag), steps the device mirrors exactly as pic_srpic_step does, and
-// copies the results out (J, EB and the species' arrays).
+// copies the results out (J, EB and the species' arrays; the weights only on
+// steps that sort, the one phase that changes them).
 //
 // The copies are pipelined against the compute and against each other:
 //   - A species binned by the tiled sort is cut into up to kChunks groups of
@@ -51,6 +52,8 @@ struct Slot {
   void*  host;
   void*  dev;
   size_t bytes;
+  bool   sort_only = false;  // changed only by a sort (the weights): copied
+                             // out only on steps that sort
 };
 }  // namespace
 
@@ -96,7 +99,7 @@ void species_slots(const pic_grid& g, const pic_species& h, const pic_species& d
     if ((a == 2 || a == 5) && g.dim != 3) continue;
     const size_t off = (size_t)p0 * es[a];
     out.push_back({ hs[a] ? (char*)hs[a] + off : nullptr, ds[a] ? (char*)ds[a] + off : nullptr,
-                    n * es[a] });
+                    n * es[a], a == 9 });
   }
 }
 
@@ -288,6 +291,9 @@ int pic_srpic_step_host(pic_ctx* ctx, pic_host_pipe* p, pic_species* hsp, pic_sp
   cudaStream_t s   = (cudaStream_t)stream;
   const size_t rb  = (size_t)g.real_bytes;
   const bool   dep = prm->deposit_enabled != 0, fs = prm->fieldsolver_enabled != 0;
+  const bool   sorts = nspecies > 0 &&
+                     ((prm->clear_interval > 0 && step % prm->clear_interval == 0 && step > 0) ||
+                      (prm->sort_interval > 0 && step % prm->sort_interval == 0));
 #define PIC_TRY(x)            \
   do {                        \
     if ((st = (x)) != PIC_OK) \
@@ -342,6 +348,14 @@ int pic_srpic_step_host(pic_ctx* ctx, pic_host_pipe* p, pic_species* hsp, pic_sp
   auto copy_out = [&](size_t a0, size_t a1, int64_t& bytes) {
     for (size_t a = a0; a < a1; ++a) {
       cudaStream_t q = a < 2 ? p->down_f : p->down;
+      if (slots[a].sort_only && !sorts) {
+        // a step without a sort leaves the range as it came in, so the host
+        // copy is current; the event still marks the end of the step's use
+        // of the device range for the next call's input copy
+        if (cudaEventRecord(p->out_done[a], q) != cudaSuccess) return false;
+        p->pending[a] = 1;
+        continue;
+      }
       const cudaError_t e =
         a < 2 ? copy_field(slots[a].host, slots[a].dev, slots[a].bytes, cudaMemcpyDeviceToHost, q)
         : slots[a].bytes > 0
@@ -395,9 +409,6 @@ int pic_srpic_step_host(pic_ctx* ctx, pic_host_pipe* p, pic_species* hsp, pic_sp
   dom.dim  = g.dim;
   dom.species.assign(dsp, dsp + nspecies);
   const bool f64   = g.real_bytes == 8;
-  const bool sorts = nspecies > 0 &&
-                     ((prm->clear_interval > 0 && step % prm->clear_interval == 0 && step > 0) ||
-                      (prm->sort_interval > 0 && step % prm->sort_interval == 0));
   // a group leaves as soon as its push ends unless the sort moves it later
   const bool early = dep && !sorts;
   auto mark = [&](int phase, int end) { return pic_timer_mark(ctx, phase, end, stream); };

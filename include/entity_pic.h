@@ -378,7 +378,8 @@ int pic_host_pipe_sync(pic_host_pipe* pipe);
  * 256 MiB). Fewer, larger groups suit small species; more groups overlap the
  * copies and the push more finely. */
 int pic_host_pipe_set_groups(pic_host_pipe* pipe, int32_t max_groups, int64_t min_group_bytes);
-/* Bytes the last pic_srpic_step_host call copied host to device and back. */
+/* Bytes the last pic_srpic_step_host call copied host to device and back
+ * (steps that sort copy the weights out as well). */
 int pic_host_pipe_bytes(const pic_host_pipe* pipe, int64_t* bytes_in, int64_t* bytes_out);
 
 /* One pic_srpic_step with host arrays as source and sink: hsp[k] (pinned host)
@@ -386,7 +387,9 @@ int pic_host_pipe_bytes(const pic_host_pipe* pipe, int64_t* bytes_in, int64_t* b
  * and hJ / dJ likewise, buff is device scratch. Copied in: EB and each
  * species' i, dx, u, weight and tag (the prev arrays stay on the device, as
  * the step rewrites them before reading). Copied out: J, EB and the same
- * species arrays, with npart updated in both descriptions. Each array's
+ * species arrays, with npart updated in both descriptions; the weights only
+ * on steps that sort (or clear), since no other phase changes them and the
+ * host copy is otherwise current. Each array's
  * input copy waits only for the previous call's output copy of that array,
  * so one step's device-to-host copies overlap the next step's host-to-device
  * copies. Asynchronous: the host arrays hold the result after

@@ -29,12 +29,16 @@ def _pinned(sp):
                          sp.pusher, sp.npart, sp.index)
 
 
+@pytest.mark.parametrize("nsteps", [9, 10])
 @pytest.mark.parametrize("dim,sort_tiled,clear,deposit", [
     (2, False, 100, True), (3, False, 100, True), (2, True, 100, True), (3, True, 3, True),
     (2, True, 100, False)])
-def test_host_resident_steps_match_device_steps(dim, sort_tiled, clear, deposit):
+def test_host_resident_steps_match_device_steps(dim, sort_tiled, clear, deposit, nsteps):
     """Tiled sorts split each species into tile groups that are copied and
-    pushed one by one; dead removal changes the counts and the groups."""
+    pushed one by one; dead removal changes the counts and the groups. The
+    weights go back to the host only on steps that sort (the last step sorts
+    with 9 steps, not with 10 unless it clears), and end up equal all the
+    same."""
     n = (32, 24, 1) if dim == 2 else (16, 16, 8)
     g = GridSpec(dim=dim, n=n, order=2, real=torch.float64)
     prm = step_params(g, cfl=0.45, ppc0=8.0, skindepth0=4.0, larmor0=3.0, nfilter=2,
@@ -49,7 +53,6 @@ def test_host_resident_steps_match_device_steps(dim, sort_tiled, clear, deposit)
     ctx = Context(g)
     da = [s.clone().to("cuda") for s in sps]
     EBa, Ja, Ba = EB0.cuda(), empty_field(g, 3, "cuda"), empty_field(g, 3, "cuda")
-    nsteps = 9
     for k in range(nsteps):
         ctx.step(da, EBa, Ja, Ba, prm, k)
     # host-resident: the state lives in pinned memory; the device arrays are
@@ -66,6 +69,7 @@ def test_host_resident_steps_match_device_steps(dim, sort_tiled, clear, deposit)
     pipe = HostPipe()
     pipe.set_groups(4, 1)   # small species: still several groups each
     for k in range(nsteps):
+        n_in = [h.npart for h in hs]  # the last call copies these counts in
         ctx2.step_host(pipe, hs, ds, hEB, EBb, hJ, Jb, Bb, prm, k)
     pipe.sync()
     torch.cuda.synchronize()
@@ -76,7 +80,9 @@ def test_host_resident_steps_match_device_steps(dim, sort_tiled, clear, deposit)
     assert float((hEB - EBa.cpu()).abs().max()) <= 1e-10 * scale
     assert float((hJ - Ja.cpu()).abs().max()) <= 1e-10 * max(float(Ja.abs().max()), 1e-30)
     rb = 8
-    want_in = hEB.numel() * rb
+    per = dim * 8 + 4 * rb + 2  # i, dx, u, w, tag
+    want_in = hEB.numel() * rb + sum(n * per for n in n_in)
+    want_out = hEB.numel() * rb
     for a, h in zip(da, hs):
         assert h.npart == a.npart
         m = a.npart
@@ -86,8 +92,12 @@ def test_host_resident_steps_match_device_steps(dim, sort_tiled, clear, deposit)
         for d in range(3):
             assert torch.allclose(h.u[d][:m], a.u[d][:m].cpu(), rtol=1e-10, atol=1e-12)
         assert torch.equal(h.tag[:m], a.tag[:m].cpu())
-        want_in += m * (dim * 8 + 4 * rb + 2)
+        assert torch.equal(h.w[:m], a.w[:m].cpu())
+        want_out += m * per
+    last = nsteps - 1
+    last_sorts = last % 2 == 0 or (last % clear == 0 and last > 0)
+    weights_out = 0 if last_sorts else sum(h.npart * rb for h in hs)
     assert nin == want_in
-    assert nout == want_in + (hJ.numel() * rb if deposit else 0)
+    assert nout == want_out - weights_out + (hJ.numel() * rb if deposit else 0)
     if clear == 3:
         assert all(h.npart < s.npart for h, s in zip(hs, sps))  # the dead were removed
