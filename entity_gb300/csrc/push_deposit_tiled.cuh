@@ -126,8 +126,9 @@ struct TileShape {
 // 3D FP32 at order 3: 8^3 cells, so that two copies of the J window fit
 // (measured on the 96^3 sweep plasma, 2 x 32 ppc: 28.1 ms per step against
 // 34.7 ms with one copy and 16 x 8 x 4 tiles). At order 2 the copies did not
-// pay (50.5 against 48.1 ms on the 256^3 turbulence plasma, 2 x 8 ppc): its
-// warps span several cells, so fewer lanes share a word.
+// pay (50.5 against 48.1 ms on the 256^3 turbulence plasma, 2 x 8 ppc; with
+// the deposit records and the even-odd rows 34.5 against 28.8 ms): its warps
+// span several cells, so fewer lanes share a word.
 // Threads per CTA: one CTA per SM (the shared memory), so the thread count
 // sets the warps that hide the kernel's latencies, and the register file
 // sets what each may use. Push+deposit of the 256^3 turbulence plasma
