@@ -228,12 +228,13 @@ int run_tiled(pic_ctx* c, const std::vector<const pic_species*>& sps, const void
     const int64_t ppc = np / std::max<int64_t>(1, (int64_t)a.nsp * cells);
     a.lane_stride     = ppc >= 24 ? 4 : (ppc >= 12 ? 2 : 1);
   }
-  if (D == 3 && sizeof(real) == 4 && O >= 1) {
-    // two buffers per SM: the launcher checks them against the kernel's
-    // occupancy and deposits directly when they do not suffice
-    const int cap = O == 3 ? 2 * pic::kStageCap : pic::kStageCap;
+  if (sizeof(real) == 4 && O >= 1 && (D == 3 || O <= 2)) {
+    // 3D: two buffers per SM (one CTA per SM); 2D: eight smaller ones (up to
+    // five CTAs per SM). The launcher checks them against the kernel's
+    // occupancy and deposits directly when they do not suffice.
+    const int cap = D == 2 ? pic::kStageCap / 4 : (O == 3 ? 2 * pic::kStageCap : pic::kStageCap);
     if (!c->stage_rec) {
-      const int n = 2 * pic::sm_count();
+      const int n = (D == 2 ? 8 : 2) * pic::sm_count();
       if (cudaMalloc((void**)&c->stage_rec, sizeof(uint4) * 2 * (size_t)cap * n) !=
               cudaSuccess ||
           cudaMalloc((void**)&c->stage_claim, sizeof(unsigned) * (size_t)n) != cudaSuccess ||

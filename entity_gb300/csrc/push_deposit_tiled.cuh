@@ -167,7 +167,8 @@ struct TiledSpecies {
   unsigned*      ovf_count;
 };
 
-// Deposit records (3D FP32, orders 1-3). Most particles end a step with
+// Deposit records (FP32: 3D orders 1-3, 2D orders 1-2; 2D records carry the
+// out-of-plane velocity in place of the third offsets). Most particles end a step with
 // both shape supports starting at the same node on every axis
 // (support_unmoved): their Esirkepov box is (O + 1) wide on each axis, a
 // stencil the compiler unrolls to its exact extent (54 of the 144 entries at
@@ -249,7 +250,8 @@ struct TiledGeom {
   // (theta = 1, 8^3-cell tiles of 2 x 32 ppc) moves 40 % of its supports;
   // with 8192 records per buffer its push+deposit on 96^3 went from 25.0 to
   // 27.5 ms, with 16384 (and the lane stride) from 20.5 to 19.6 ms
-  static constexpr bool   STAGE      = D == 3 && sizeof(real) == 4 && O >= 1;
+  // 2D at order 3 would spill at its four CTAs per SM, so it deposits at once
+  static constexpr bool   STAGE      = sizeof(real) == 4 && O >= 1 && (D == 3 || O <= 2);
   // the copies start 16 banks apart: one word in both copies falls in
   // two different banks
   static constexpr int    COPY       = WORDS * PLANE + ((16 - (WORDS * PLANE) % 32) + 32) % 32;
@@ -450,7 +452,6 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
   const int wid     = (int)(threadIdx.x >> 5);
   const int local   = (wid / ls) * (32 * ls) + ls * (int)(threadIdx.x & 31) + wid % ls;
   uint4*    recs    = slot >= 0 ? a.st.rec + (size_t)slot * a.st.cap * 2 : nullptr;
-  const real vz[3]  = { 0, 0, 0 };  // the 3D Esirkepov deposit reads no velocity
   // cell of a record relative to the tile: 8 bits per axis, offset by 64
   static_assert(G::TX + kDriftMargin + 2 < 64 && G::TY + kDriftMargin + 2 < 64 &&
                     G::TZ + kDriftMargin + 2 < 64,
@@ -563,8 +564,11 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
       };
       if constexpr (G::STAGE) {
         if (recs) {
+          // the 2D deposit reads the out-of-plane velocity, the 3D one none
+          real vp[3] = { 0, 0, 0 };
+          if constexpr (D == 2) deposit_velocity<D, real>(q, a.dx, vp);
           if (support_unmoved<D, O, real>(q)) {
-            deposit_with_velocity<D, O, real, true>(q, vz, wp, S.charge, a.inv_dt, ng, nullptr,
+            deposit_with_velocity<D, O, real, true>(q, vp, wp, S.charge, a.inv_dt, ng, nullptr,
                                                     add);
             continue;
           }
@@ -587,11 +591,14 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
                 cells |= ((unsigned)(q.i[d] - T0[d] + 64) << (8 * d)) |
                          ((unsigned)(q.ip[d] - q.i[d] + 1) << (24 + 2 * d));
               const float coeff = (float)(wp * S.charge);
+              // 3D: the offsets x3 in the third words; 2D: the out-of-plane
+              // velocity in their place
+              const float w3 = D == 3 ? q.dx[2] : (float)vp[2], p3 = D == 3 ? q.dxp[2] : 0.f;
               __stcg(recs + 2 * r, make_uint4(cells, __float_as_uint(q.dx[0]),
-                                              __float_as_uint(q.dx[1]), __float_as_uint(q.dx[2])));
+                                              __float_as_uint(q.dx[1]), __float_as_uint(w3)));
               __stcg(recs + 2 * r + 1,
                      make_uint4(__float_as_uint(q.dxp[0]), __float_as_uint(q.dxp[1]),
-                                __float_as_uint(q.dxp[2]), __float_as_uint(coeff)));
+                                __float_as_uint(p3), __float_as_uint(coeff)));
               continue;
             }
           }
@@ -617,6 +624,7 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
         Prtl<real>  q;
         const float dx[3]  = { __uint_as_float(u0.y), __uint_as_float(u0.z), __uint_as_float(u0.w) };
         const float dxp[3] = { __uint_as_float(u1.x), __uint_as_float(u1.y), __uint_as_float(u1.z) };
+        const real  vp[3]  = { 0, 0, D == 2 ? (real)dx[2] : (real)0 };
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           q.i[d]   = (int)((u0.x >> (8 * d)) & 255u) - 64 + T0[d];
@@ -624,7 +632,7 @@ __global__ void __launch_bounds__(TileShape<D, real, O>::NT, TileShape<D, real, 
           q.dx[d]  = dx[d];
           q.dxp[d] = dxp[d];
         }
-        deposit_with_velocity<D, O, real>(q, vz, (real)__uint_as_float(u1.w), (real)1, a.inv_dt,
+        deposit_with_velocity<D, O, real>(q, vp, (real)__uint_as_float(u1.w), (real)1, a.inv_dt,
                                           ng, nullptr, add);
         // Lanes 4m..4m+3 have read the four records of one 128-byte line and
         // used them: the line is dropped from L2 unwritten, so the records

@@ -238,19 +238,22 @@ def test_exact_current_accumulation_adds_to_J():
     assert torch.equal(Ja, J0 + Jz)
 
 
-@pytest.mark.parametrize("order,ppc,temp", [(1, 4, 0.3), (2, 4, 0.05), (2, 4, 2.0),
-                                            (3, 4, 0.3), (1, 12, 2.0), (2, 12, 2.0),
-                                            (3, 24, 2.0)])
-def test_deposit_records_leave_J_unchanged(order, ppc, temp, monkeypatch):
-    """3D FP32, orders 1-3: the particles whose shape support moved are
-    deposited from records after the tile's pushes, the others at once
-    through the narrow stencil. J is the same to the bit as with every particle deposited at
-    once (ENTITY_PIC_NO_RECORDS=1), because the window's integer sums do not
+@pytest.mark.parametrize("dim,order,ppc,temp", [
+    (3, 1, 4, 0.3), (3, 2, 4, 0.05), (3, 2, 4, 2.0), (3, 3, 4, 0.3), (3, 1, 12, 2.0),
+    (3, 2, 12, 2.0), (3, 3, 24, 2.0), (2, 1, 16, 0.3), (2, 2, 8, 0.3), (2, 1, 16, 2.0)])
+def test_deposit_records_leave_J_unchanged(dim, order, ppc, temp, monkeypatch):
+    """FP32, 3D orders 1-3 and 2D orders 1-2: the particles whose shape
+    support moved are deposited from records after the tile's pushes, the
+    others at once through the narrow stencil. J is the same to the bit as
+    with every particle deposited at once (ENTITY_PIC_NO_RECORDS=1), because
+    the window's integer sums do not
     depend on the order of the additions; the particles are identical. The
-    hot 2 x 12 ppc (orders 1-2) and 2 x 24 ppc (order 3) cases fill a tile's
-    record buffer past its capacity, so the particles beyond it are
-    deposited at once as well."""
-    g = GridSpec(dim=3, n=(32, 16, 16), order=order, real=torch.float32)
+    hot 3D 2 x 12 ppc (orders 1-2), 2 x 24 ppc (order 3) and 2D 2 x 16 ppc
+    cases fill a tile's record buffer past its capacity, so the particles
+    beyond it are deposited at once as well. The 2D records carry the
+    out-of-plane velocity of the third current component."""
+    n = (32, 16, 16) if dim == 3 else (96, 64, 1)
+    g = GridSpec(dim=dim, n=n, order=order, real=torch.float32)
     EB = random_fields(g, 37, amp=0.1).cuda()
     ctx = Context(g)
     gpu = []
@@ -274,7 +277,7 @@ def test_deposit_records_leave_J_unchanged(order, ppc, temp, monkeypatch):
         assert torch.equal(Ja, Jb)
         assert float(Ja.abs().max()) > 0
     for a, b in zip(runs[0][0], runs[1][0]):
-        _assert_particles_equal(a.to("cpu"), b, 3)
+        _assert_particles_equal(a.to("cpu"), b, dim)
     assert ctx.device_errors() == [0, 0, 0, 0]
     assert ctx.wait_timeouts() == 0
 
