@@ -64,8 +64,8 @@ struct pic_ctx {
   long long*                                      jfix       = nullptr;
   size_t                                          jfix_elems = 0;
   unsigned*                                       jfix_bound = nullptr;
-  // deposit records of the tiled kernel (3D FP32; allocated on first use):
-  // stage_slots buffers of pic::kStageCap records and their claim words
+  // deposit records of the tiled kernel (FP32; allocated on first use):
+  // stage_slots buffers and their claim words (sizes: run_tiled)
   uint4*                                          stage_rec   = nullptr;
   unsigned*                                       stage_claim = nullptr;
   int                                             stage_slots = 0;
