@@ -278,6 +278,44 @@ def test_sort_bins_and_dead_last(dim):
     assert torch.equal(sp.u[0], before_u[perm])
 
 
+@pytest.mark.parametrize("dim,tile", [(2, (4, 3, 1)), (3, (4, 2, 3)), (3, (5, 2, 2))])
+def test_tiled_sort_order(dim, tile):
+    # the tile-major key of PIC_SORT_TILED: tiles i1-fastest, then the cell in
+    # the tile i1-fastest with each row's even cells before its odd ones
+    # (an odd row width puts the extra even cell first); stable, dead last
+    n = (9, 7, 1) if dim == 2 else (9, 5, 7)
+    g = GridSpec(dim=dim, n=n, order=1, real=torch.float32)
+    gen = torch.Generator()
+    gen.manual_seed(11)
+    npart = 800
+    cells = [tuple(int(torch.randint(0, n[a], (1,), generator=gen)) for a in range(dim))
+             for _ in range(npart)]
+    tags = [int(torch.rand(1, generator=gen) > 0.1) for _ in range(npart)]
+    sp = species_from_lists(g, cells, [tuple(0.5 for _ in range(dim))] * npart,
+                            [(float(k), 0.0, 0.0) for k in range(npart)], tags=tags)
+    perm = Oracle(g).sort_tiled(sp, tile)
+    ts = [tile[a] if a < dim else 1 for a in range(3)]
+    nt = [-(-(n[a] if a < dim else 1) // ts[a]) for a in range(3)]
+    keys = []
+    for p in range(npart):
+        if int(sp.tag[p]) != 1:
+            keys.append((1,))
+            continue
+        c = [int(sp.i[a][p]) if a < dim else 0 for a in range(3)]
+        t = ((c[2] // ts[2]) * nt[1] + c[1] // ts[1]) * nt[0] + c[0] // ts[0]
+        lx = c[0] % ts[0]
+        slot = lx // 2 if lx % 2 == 0 else (ts[0] + 1) // 2 + lx // 2
+        keys.append((0, t, c[2] % ts[2], c[1] % ts[1], slot))
+    assert keys == sorted(keys)
+    for a in range(npart - 1):
+        if keys[a] == keys[a + 1]:
+            assert int(perm[a]) < int(perm[a + 1])
+    # the slot is a permutation of the row
+    for w in (ts[0],):
+        slots = sorted(x // 2 if x % 2 == 0 else (w + 1) // 2 + x // 2 for x in range(w))
+        assert slots == list(range(w))
+
+
 def test_remove_dead_compacts_in_order():
     g = GridSpec(dim=2, n=(4, 4, 1), order=1, real=torch.float64)
     tags = [1, 0, 1, 1, 0, 0, 1, 0]
