@@ -168,8 +168,8 @@ struct TiledSpecies {
 };
 
 // Deposit records (FP32: 3D orders 1-3, 2D orders 1-2; 2D records carry the
-// out-of-plane velocity in place of the third offsets). Most particles end a step with
-// both shape supports starting at the same node on every axis
+// out-of-plane velocity in place of the third offsets). Most particles end a
+// step with both shape supports starting at the same node on every axis
 // (support_unmoved): their Esirkepov box is (O + 1) wide on each axis, a
 // stencil the compiler unrolls to its exact extent (54 of the 144 entries at
 // order 2). A warp deposits those at once. The others, whose box is O + 2
@@ -185,7 +185,8 @@ struct DepStage {
   unsigned* claim  = nullptr;  // nslots words: 0 free, 1 held
   int       nslots = 0, cap = 0;
 };
-constexpr int kStageCap = 8192;  // records per buffer (256 KB), twice that at order 3
+// records per 3D buffer (256 KB); twice that at order 3, a quarter in 2D
+constexpr int kStageCap = 8192;
 
 // drops the 128-byte line at p (128-byte aligned) from L2 without writing it
 // back; its contents are undefined until written again
