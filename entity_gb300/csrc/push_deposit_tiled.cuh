@@ -10,7 +10,7 @@
 //      across a periodic edge;
 //   2. pushes every particle of the tile (all species) gathering E/B from
 //      shared memory and depositing its current into a shared-memory J window
-//      (tile + deposit halo + margin); in 3D FP32 a particle whose shape
+//      (tile + deposit halo + margin); in FP32 a particle whose shape
 //      support moved is deposited after the pushes, from a record (DepStage),
 //   3. adds the J window to global J once, wrapping periodic images onto
 //      their active cells (the fold SynchronizeFields performs in the
