@@ -206,6 +206,10 @@ class ClockSampler:
                 "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows)}
 
 
+# GB300's nominal HBM3e bandwidth, shown beside the measured denominator
+HBM_NOMINAL_GBS = 8000.0
+
+
 def hbm_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -510,6 +514,7 @@ def run_ours(args, w):
         "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in phases.items()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
+                     "frac_of_nominal_8tbs": achieved / HBM_NOMINAL_GBS,
                      "kernel": "k_push_deposit_tiled (fused push + deposit, both species, "
                                "plus the overflow-list drain)",
                      "bytes_per_launch": bytes_pd, "launch_ms": pd_ms / pd_n,
@@ -796,6 +801,7 @@ def run_sweep(args, w):
         "phases_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in phases.items()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
+                     "frac_of_nominal_8tbs": achieved / HBM_NOMINAL_GBS,
                      "kernel": "k_push_deposit_tiled (FP32, both species)",
                      "bytes_per_launch": bytes_pd, "launch_ms": pd_ms / pd_n,
                      "binding_pipes": PIPE_LIMITS.get("sweep3d"),
